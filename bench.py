@@ -1,0 +1,394 @@
+#!/usr/bin/env python3
+"""Benchmark of the periodic FE stiffness operator on one GB300.
+
+Default workload (one "step" = one operator application f = K u):
+3D hexahedral periodic grid 128 x 128 x 128, cubic cells h = 1/128,
+mu = 1.0, nu = 0.25, FP64, u (3 components per node) ~ N(0, 1) from seed 1
+with the mean removed per component.  Metric: operator GDoF/s (DoF = 3 x
+128^3 per application) with the HBM roofline fraction of the dominant
+kernel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload operator|operator_f32|cg|serve|aniso]
+
+Multi-GPU (torchrun): every rank runs an independent replica ("replicas
+only": the operator does not shard across GPUs here); value = DoF processed
+by all ranks / max-over-ranks time.
+
+--impl reference times the reference's CPU path for the same workload (the
+oracle restatement of compute_Ku, tests/test_bri17.cpp:56-107, with
+numpy/scipy FFTs in place of FFTW) on all host cores, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+METRIC = "operator GDoF/s (% HBM peak); CG solves/s at 1e-8 vs FP64; p50/p99 latency"
+L2_BYTES = 129 * 1024 * 1024
+WORKLOAD_128 = dict(shape=(128, 128, 128), L=(1.0, 1.0, 1.0), mu=1.0, nu=0.25, seed=1)
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"bri17_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for name, val in zip(names, p[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_u(shape, seed, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal((len(shape),) + tuple(shape))
+    u -= u.reshape(len(shape), -1).mean(axis=1).reshape((len(shape),) + (1,) * len(shape))
+    return u.astype(dtype)
+
+
+def fp64_peak_live(torch):
+    """FP64 throughput of cuBLAS DGEMM on this GPU (TFLOP/s), measured live
+    as the FP64 compute roofline denominator."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/traffic.json), scaled as recorded there; None if absent."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        return d[workload][kernel]["dram_bytes_per_launch"]
+    except Exception:
+        return None
+
+
+def pass_bytes(geom_dim, dof, cspec, comps, scalar):
+    """Algorithmic bytes per launch of each pass: every pass reads its input
+    array once and writes its output array once."""
+    csz = 2 * scalar
+    spec = comps * cspec * csz
+    field = dof * scalar
+    return {"rows_r2c": field + spec, "axis_c2c_fwd": 2 * spec, "axis0_fused": 2 * spec,
+            "axis_c2c_inv": 2 * spec, "rows_c2r": spec + field}
+
+
+def fused_flops(shape, comps):
+    """Conventional flop count of one axis0_fused launch: 5 n log2 n per
+    complex transform (forward + inverse per component per line) plus ~56
+    flops per mode for K(k) and the 3x3 product."""
+    import math
+    n0 = shape[0]
+    lines = int(np.prod(shape[1:-1])) * (shape[-1] // 2 + 1) if len(shape) == 3 else shape[-1] // 2 + 1
+    per_line = 2 * comps * 5 * n0 * math.log2(n0) + 56 * n0
+    return lines * per_line
+
+
+# ---------------------------------------------------------------------------
+
+
+def cpu_reference_apply_time(workload, threads: int, reps: int):
+    """Time the oracle restatement of compute_Ku on the host: C2C FFTs
+    (numpy pocketfft single-threaded, or scipy.fft with `threads` workers)
+    plus the per-mode loop in C with `threads` OpenMP threads."""
+    from oracle import oracle as O
+    shape = workload["shape"]
+    grid = O.Grid(shape, workload["L"])
+    h = O.Hooke(workload["mu"], workload["nu"], grid)
+    u = make_u(shape, workload["seed"])
+    O.set_num_threads(threads)
+    axes = tuple(range(1, len(shape) + 1))
+    fft_mod = None
+    if threads > 1:
+        try:
+            import scipy.fft as sf
+            fft_mod = sf
+        except Exception:
+            fft_mod = None
+
+    def apply():
+        uc = u.astype(np.complex128)
+        if fft_mod is not None:
+            uhat = fft_mod.fftn(uc, axes=axes, workers=threads)
+        else:
+            uhat = np.fft.fftn(uc, axes=axes)
+        kuhat = h._modal_loop(O.lib().oracle_stiffness_modal_apply, uhat, grid.dim)
+        if fft_mod is not None:
+            ku = fft_mod.ifftn(kuhat, axes=axes, norm="forward", workers=threads)
+        else:
+            ku = np.fft.ifftn(kuhat, axes=axes, norm="forward")
+        ku *= grid.cell_volume / grid.size
+        return ku.real
+
+    apply()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        apply()
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if ws > 1 and rank != 0:
+        return 0
+    w = WORKLOAD_128
+    dof = 3 * int(np.prod(w["shape"]))
+    threads = os.cpu_count() or 1
+    # Warm-up then K timed steps; each step = one full application.
+    times = cpu_reference_apply_time(w, threads, max(1, args.steps))
+    total = sum(times)
+    value = dof * len(times) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GDoF/s",
+        "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(w, args.gpus),
+        "cpu_baseline": {"value": value, "unit": "GDoF/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} full 128^3 FP64 applications "
+                                   "(C2C scipy.fft + OpenMP per-mode loop)"},
+        "e2e": {"value": value, "unit": "GDoF/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_of(w, ngpus, precision="f64"):
+    shape = w["shape"]
+    return {"workload": f"operator f = K u, 3D hexahedral periodic grid "
+                        f"{shape[0]}x{shape[1]}x{shape[2]}, h=1/{shape[0]}, "
+                        f"mu={w['mu']} nu={w['nu']}, {precision.upper()}, u~N(0,1) seed "
+                        f"{w['seed']} mean-free",
+            "grid": list(shape), "dof_per_step": 3 * int(np.prod(shape)),
+            "parallelism": f"replicas x{ngpus}",
+            "l2": "inputs rotate over buffer sets larger than L2"}
+
+
+def run_operator(args, precision="f64"):
+    import torch
+
+    from bri17_gb300 import CartesianGrid, Hooke, _lib
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = WORKLOAD_128
+    shape = w["shape"]
+    dim = len(shape)
+    dof = dim * int(np.prod(shape))
+    hooke = Hooke(w["mu"], w["nu"], CartesianGrid(shape, w["L"]), precision=precision)
+    tdt = torch.float64 if precision == "f64" else torch.float32
+    scalar = 8 if precision == "f64" else 4
+    u0 = torch.from_numpy(make_u(shape, w["seed"])).to(device="cuda", dtype=tdt)
+    per_set = 2 * dof * scalar
+    nrot = max(2, -(-3 * L2_BYTES // per_set))
+    us = [u0.clone() for _ in range(nrot)]
+    fs = [torch.empty_like(u0) for _ in range(nrot)]
+    stream = torch.cuda.current_stream()
+    L = _lib.load()
+    for i in range(args.warmup):
+        hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
+    torch.cuda.synchronize()
+    L.bri17_op_set_pass_timing(hooke.handle, 1)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ms_total = e0.elapsed_time(e1)
+    import ctypes
+    pms = (ctypes.c_double * 5)()
+    pn = (ctypes.c_int64 * 5)()
+    npass = ctypes.c_int()
+    L.bri17_op_pass_times(hooke.handle, pms, pn, 5, ctypes.byref(npass))
+    L.bri17_op_set_pass_timing(hooke.handle, 0)
+    passes = {L.bri17_pass_name(i).decode(): {"ms_total": pms[i], "launches": pn[i]}
+              for i in range(5) if pn[i] > 0}
+    t_max = ms_total
+    if ws > 1:
+        t = torch.tensor([ms_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ws * dof * args.steps / (t_max * 1e-3) / 1e9
+    # Correctness of the timed output (first set) against a fresh apply.
+    check = hooke.apply_stiffness(us[0])
+    assert torch.equal(check, fs[0]) or args.steps == 0
+
+    # End to end through the host-buffer C-ABI entry point (pinned memory).
+    u_host = us[0].cpu().pin_memory()
+    f_host = torch.empty_like(u_host).pin_memory()
+    import ctypes as C
+    sp = C.c_void_p(stream.cuda_stream)
+    for _ in range(max(1, args.warmup)):
+        _lib.check(L.bri17_apply_stiffness_host(hooke.handle, C.c_void_p(u_host.data_ptr()),
+                                                C.c_void_p(f_host.data_ptr()), sp), "host")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.bri17_apply_stiffness_host(hooke.handle, C.c_void_p(u_host.data_ptr()),
+                                     C.c_void_p(f_host.data_ptr()), sp)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": dof * args.steps / e2e_s / 1e9, "unit": "GDoF/s",
+           "h2d_bytes_per_step": dof * scalar, "d2h_bytes_per_step": dof * scalar}
+
+    hbm_peak, peak_kind = peaks()
+    cspec = shape[0] * shape[1] * (shape[2] // 2 + 1)
+    pb = pass_bytes(dim, dof, cspec, dim, scalar)
+    dom = max(passes, key=lambda k: passes[k]["ms_total"]) if passes else None
+    roof = None
+    extra = {}
+    if dom:
+        avg_ms = passes[dom]["ms_total"] / passes[dom]["launches"]
+        ach = pb[dom] / (avg_ms * 1e-3) / 1e9
+        wl = f"{precision}_128cubed"
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm_peak,
+                "traffic": traffic_from_profiles(dom, wl),
+                "algorithmic_bytes_per_launch": pb[dom], "avg_launch_ms": avg_ms}
+        if dom == "axis0_fused":
+            flops = fused_flops(shape, dim)
+            if precision == "f64":
+                p64 = fp64_peak_live(torch)
+                extra["fp64_roofline"] = {
+                    "kernel": dom, "achieved_tflops": flops / (avg_ms * 1e-3) / 1e12,
+                    "peak_tflops": p64, "peak_kind": "cuBLAS DGEMM measured live",
+                    "frac": flops / (avg_ms * 1e-3) / 1e12 / p64,
+                    "flops_per_launch": flops, "flop_model": "5 n log2 n per complex "
+                    "transform + 56 per mode"}
+        extra["operator_hbm_frac"] = 2 * dof * scalar / (ms_total / args.steps * 1e-3) / 1e9 / hbm_peak
+    line = {
+        "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": precision, "data": "synthetic", "config": config_of(w, ws, precision),
+        "roofline": roof, "e2e": e2e, "gpu_launches": sum(p["launches"] for p in passes.values()),
+        "clocks": clocks, "passes": passes, **extra,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        times = cpu_reference_apply_time(w, 1, 2)
+        line["cpu_baseline"] = {
+            "value": dof * len(times) / sum(times) / 1e9, "unit": "GDoF/s", "cores": 1,
+            "kind": "port", "sample": f"{len(times)} full 128^3 applications, 1 thread, "
+                                      "C2C numpy FFT + per-mode loop (reference-faithful)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="operator", choices=["operator", "operator_f32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.workload == "operator_f32":
+        return run_operator(args, precision="f32")
+    return run_operator(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,678 @@
+// cg.cu -- conjugate-gradient solvers of K x = b on the periodic stiffness
+// operator (new: the reference stops at the per-mode solve
+// Hooke::modal_eigenstress_to_opposite_strain, include/bri17/bri17.hpp:
+// 308-355, which serves as the exact oracle of these solves).
+//
+// Plain mode runs CG in the handle's precision.  Mixed mode runs an FP32 CG
+// on the FP32 twin of the operator inside an FP64 iterative-refinement loop:
+// residual r = b - K x, zero-mean projection and the correction x += d are
+// FP64.  Scalars (rr, pq, alpha, beta) stay on the device, reductions are
+// deterministic (per-block partials summed in a fixed order by the last
+// block), and a chunk of iterations is replayed as one CUDA graph between
+// host checks of the residual.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "op.cuh"
+
+namespace bri17gb {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedMaxBlocks = 1024;
+constexpr int kChunk = 8;  // CG iterations per graph replay
+
+struct CgState {
+  double rr;      // r.r of the current iterate
+  double pq;      // p.K p
+  double alpha;
+  double beta;
+  double thresh;  // stop when rr <= thresh
+  double aux;     // scratch result of helper reductions
+  double mean[6]; // per-component means (projection)
+  int active;     // 1 while iterating
+  int flag;       // BRI17_OK or BRI17_ERR_BREAKDOWN
+  int iters;
+  int pad;
+  unsigned int counter;  // last-block ticket
+  unsigned int pad2;
+};
+
+static int red_blocks(int64_t n) {
+  int64_t b = (n + kRedThreads * 4 - 1) / (kRedThreads * 4);
+  if (b < 1) b = 1;
+  if (b > kRedMaxBlocks) b = kRedMaxBlocks;
+  return (int)b;
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sh[kRedThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = l < kRedThreads / 32 ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+// Writes this block's partial; returns true in every thread of the last
+// block to finish, with *total = fixed-order sum of all partials.
+__device__ bool last_block_total(double v, double* partials,
+                                 unsigned int* counter, int nparts,
+                                 double* total) {
+  __shared__ bool is_last;
+  const double b = block_sum(v);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x + blockIdx.y * gridDim.x] = b;
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    is_last = (t == (unsigned int)nparts - 1);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+    s += __ldcg(partials + i);
+  const double tot = block_sum(s);
+  if (threadIdx.x == 0) {
+    *total = tot;
+    *counter = 0u;
+  }
+  return true;
+}
+
+// pq = p . q; alpha = rr / pq; breakdown if pq <= 0 or not finite.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_dot_pq(const T* __restrict__ p, const T* __restrict__ q, int64_t n,
+             CgState* st, double* partials) {
+  if (!st->active) return;
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v += (double)p[i] * (double)q[i];
+  double tot;
+  if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
+      threadIdx.x == 0) {
+    st->pq = tot;
+    if (!(tot > 0.0) || !isfinite(tot)) {
+      st->flag = BRI17_ERR_BREAKDOWN;
+      st->active = 0;
+    } else {
+      st->alpha = st->rr / tot;
+    }
+  }
+}
+
+// x += alpha p; r -= alpha q; rr_new = r.r; beta = rr_new / rr.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+             const T* __restrict__ q, int64_t n, CgState* st,
+             double* partials) {
+  if (!st->active) return;
+  const T a = (T)st->alpha;
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    const T ri = r[i] - a * q[i];
+    r[i] = ri;
+    v += (double)ri * (double)ri;
+  }
+  double tot;
+  if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
+      threadIdx.x == 0) {
+    st->iters += 1;
+    if (!isfinite(tot)) {
+      st->flag = BRI17_ERR_BREAKDOWN;
+      st->active = 0;
+      return;
+    }
+    st->beta = tot / st->rr;
+    st->rr = tot;
+    if (tot <= st->thresh) st->active = 0;
+  }
+}
+
+// p = r + beta p.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pupdate(T* __restrict__ p, const T* __restrict__ r, int64_t n,
+              const CgState* st) {
+  if (!st->active) return;
+  const T b = (T)st->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = r[i] + b * p[i];
+}
+
+// aux = a . b
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_dot(const T* __restrict__ a, const T* __restrict__ b, int64_t n,
+          CgState* st, double* partials) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v += (double)a[i] * (double)b[i];
+  double tot;
+  if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
+      threadIdx.x == 0)
+    st->aux = tot;
+}
+
+// Per-component means of a dim x size field (grid.y = component).
+__global__ void __launch_bounds__(kRedThreads)
+    k_comp_mean(const double* __restrict__ a, int64_t size, CgState* st,
+                double* partials) {
+  const double* ac = a + (int64_t)blockIdx.y * size;
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < size;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v += ac[i];
+  // The per-component sums are finished by the last block over all
+  // components, in a fixed order.
+  __shared__ bool is_last;
+  const double b = block_sum(v);
+  const int nparts = gridDim.x * gridDim.y;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x + blockIdx.y * gridDim.x] = b;
+    __threadfence();
+    const unsigned int t = atomicAdd(&st->counter, 1u);
+    is_last = (t == (unsigned int)nparts - 1);
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int c = 0; c < (int)gridDim.y; c++) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      s += __ldcg(partials + c * gridDim.x + i);
+    const double tot = block_sum(s);
+    if (threadIdx.x == 0) st->mean[c] = tot / (double)size;
+  }
+  if (threadIdx.x == 0) st->counter = 0u;
+}
+
+__global__ void k_sub_mean(double* __restrict__ a, int64_t size,
+                           const CgState* st) {
+  const double m = st->mean[blockIdx.y];
+  double* ac = a + (int64_t)blockIdx.y * size;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < size;
+       i += (int64_t)gridDim.x * blockDim.x)
+    ac[i] -= m;
+}
+
+// r = b - Kx (Kx given), FP64.
+__global__ void k_residual(double* __restrict__ r, const double* __restrict__ b,
+                           const double* __restrict__ kx, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = b[i] - kx[i];
+}
+
+// out32 = (float)(in64 * scale); zero the FP32 iterate.
+__global__ void k_to_f32(float* __restrict__ out, const double* __restrict__ in,
+                         double scale, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)(in[i] * scale);
+}
+
+// x64 += scale * d32.
+__global__ void k_add_f32(double* __restrict__ x, const float* __restrict__ d,
+                          double scale, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += scale * (double)d[i];
+}
+
+// CG start: p = r; rr = r.r; thresh = rel_tol2 * aux (aux = b.b set by a
+// preceding k_dot); active while rr > thresh.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_start(const T* __restrict__ r, T* __restrict__ p, int64_t n, CgState* st,
+            double* partials, double rel_tol2) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T ri = r[i];
+    p[i] = ri;
+    v += (double)ri * (double)ri;
+  }
+  double tot;
+  if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
+      threadIdx.x == 0) {
+    st->rr = tot;
+    st->thresh = rel_tol2 * st->aux;
+    st->iters = 0;
+    st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
+    st->active = (tot > st->thresh && isfinite(tot)) ? 1 : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+struct CgWork {
+  int64_t n;        // dim * size
+  double* x;        // FP64 iterate (work copy)
+  double* r;        // FP64 residual
+  double* p;        // FP64 search direction (plain mode)
+  double* q;        // FP64 K p / K x
+  float* d32;       // FP32 inner iterate (mixed mode)
+  float* r32;
+  float* p32;
+  float* q32;
+  double* partials;
+  CgState* st;
+  CgState* st_host;  // pinned mirror
+  cudaStream_t stream;
+  cudaGraphExec_t graph64;
+  cudaGraphExec_t graph32;
+  unsigned epoch64;
+  unsigned epoch32;
+  bool plain_ready;
+};
+
+static void cg_free(void* p) {
+  CgWork* w = reinterpret_cast<CgWork*>(p);
+  if (!w) return;
+  if (w->stream) cudaStreamSynchronize(w->stream);
+  if (w->graph64) cudaGraphExecDestroy(w->graph64);
+  if (w->graph32) cudaGraphExecDestroy(w->graph32);
+  cudaFree(w->x);
+  cudaFree(w->r);
+  cudaFree(w->p);
+  cudaFree(w->q);
+  cudaFree(w->d32);
+  cudaFree(w->r32);
+  cudaFree(w->p32);
+  cudaFree(w->q32);
+  cudaFree(w->partials);
+  cudaFree(w->st);
+  cudaFreeHost(w->st_host);
+  if (w->stream) cudaStreamDestroy(w->stream);
+  delete w;
+}
+
+static int ensure_work(bri17_op* op, bool mixed, CgWork** out) {
+  CgWork* w = reinterpret_cast<CgWork*>(op->cg_work);
+  const int64_t n = (int64_t)op->g.dim * op->g.size;
+  if (!w) {
+    w = new CgWork();
+    memset(w, 0, sizeof(*w));
+    w->n = n;
+    op->cg_work = w;
+    op->cg_free = cg_free;
+    BRI17_CUDA_TRY(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    BRI17_CUDA_TRY(cudaMalloc(&w->x, n * sizeof(double)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->r, n * sizeof(double)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->q, n * sizeof(double)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->partials, 6 * kRedMaxBlocks * sizeof(double)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->st, sizeof(CgState)));
+    BRI17_CUDA_TRY(cudaMemset(w->st, 0, sizeof(CgState)));
+    BRI17_CUDA_TRY(cudaMallocHost(&w->st_host, sizeof(CgState)));
+    memset(w->st_host, 0, sizeof(CgState));
+  }
+  if (!mixed && !w->plain_ready) {
+    if (op->precision == BRI17_F64) {
+      BRI17_CUDA_TRY(cudaMalloc(&w->p, n * sizeof(double)));
+    } else {
+      BRI17_CUDA_TRY(cudaMalloc(&w->d32, n * sizeof(float)));
+      BRI17_CUDA_TRY(cudaMalloc(&w->r32, n * sizeof(float)));
+      BRI17_CUDA_TRY(cudaMalloc(&w->p32, n * sizeof(float)));
+      BRI17_CUDA_TRY(cudaMalloc(&w->q32, n * sizeof(float)));
+    }
+    w->plain_ready = true;
+  }
+  if (mixed && !w->d32) {  // (an FP32 handle's plain mode allocated these)
+    BRI17_CUDA_TRY(cudaMalloc(&w->d32, n * sizeof(float)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->r32, n * sizeof(float)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->p32, n * sizeof(float)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->q32, n * sizeof(float)));
+  }
+  *out = w;
+  return BRI17_OK;
+}
+
+static unsigned grid1(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+// Enqueue `chunk` CG iterations of precision T on `opk` (the operator whose
+// precision is T), then a copy of the state to the pinned mirror.
+template <typename T>
+static int enqueue_chunk(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
+                         cudaStream_t s) {
+  const int64_t n = w->n;
+  const int rb = red_blocks(n);
+  for (int it = 0; it < kChunk; it++) {
+    int rc = apply_stiffness_async(opk, p, q, s);
+    if (rc != BRI17_OK) return rc;
+    k_dot_pq<T><<<rb, kRedThreads, 0, s>>>(p, q, n, w->st, w->partials);
+    k_update<T><<<rb, kRedThreads, 0, s>>>(x, r, p, q, n, w->st, w->partials);
+    k_pupdate<T><<<grid1(n), 256, 0, s>>>(p, r, n, w->st);
+  }
+  BRI17_CUDA_TRY(cudaMemcpyAsync(w->st_host, w->st, sizeof(CgState),
+                                 cudaMemcpyDeviceToHost, s));
+  return BRI17_OK;
+}
+
+template <typename T>
+static int get_graph(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
+                     cudaGraphExec_t* exec, unsigned* epoch) {
+  if (*exec && *epoch == opk->material_epoch) return BRI17_OK;
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+  }
+  cudaGraph_t graph;
+  BRI17_CUDA_TRY(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_chunk<T>(opk, w, x, r, p, q, w->stream);
+  cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
+  if (rc != BRI17_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  *epoch = opk->material_epoch;
+  return BRI17_OK;
+}
+
+// Run CG iterations (state already started) until inactive or `budget`
+// iterations; returns the status flag.  *iters receives the count.
+template <typename T>
+static int run_cg(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
+                  cudaGraphExec_t* exec, unsigned* epoch, int budget,
+                  int* iters) {
+  int rc = get_graph<T>(opk, w, x, r, p, q, exec, epoch);
+  if (rc != BRI17_OK) return rc;
+  // The state was started on w->stream; refresh the mirror first.
+  BRI17_CUDA_TRY(cudaMemcpyAsync(w->st_host, w->st, sizeof(CgState),
+                                 cudaMemcpyDeviceToHost, w->stream));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(w->stream));
+  while (w->st_host->active && w->st_host->iters < budget) {
+    BRI17_CUDA_TRY(cudaGraphLaunch(*exec, w->stream));
+    BRI17_CUDA_TRY(cudaStreamSynchronize(w->stream));
+  }
+  *iters = w->st_host->iters;
+  if (w->st_host->flag != BRI17_OK) return w->st_host->flag;
+  return w->st_host->active ? BRI17_ERR_NOT_CONVERGED : BRI17_OK;
+}
+
+static int read_state(CgWork* w) {
+  BRI17_CUDA_TRY(cudaMemcpyAsync(w->st_host, w->st, sizeof(CgState),
+                                 cudaMemcpyDeviceToHost, w->stream));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(w->stream));
+  return BRI17_OK;
+}
+
+// x <- x - mean(x) per component (FP64).
+static void project_mean(bri17_op* op, CgWork* w, double* a) {
+  const int64_t size = op->g.size;
+  int gb = red_blocks(size);
+  if (gb > kRedMaxBlocks / 1) gb = kRedMaxBlocks;
+  dim3 grid(gb, op->g.dim);
+  k_comp_mean<<<grid, kRedThreads, 0, w->stream>>>(a, size, w->st, w->partials);
+  dim3 grid2(grid1(size), op->g.dim);
+  k_sub_mean<<<grid2, 256, 0, w->stream>>>(a, size, w->st);
+}
+
+// r = b - K x (FP64) and aux = r.r.
+static int residual64(bri17_op* op, CgWork* w, const double* b) {
+  int rc = apply_stiffness_async(op, w->x, w->q, w->stream);
+  if (rc != BRI17_OK) return rc;
+  k_residual<<<grid1(w->n), 256, 0, w->stream>>>(w->r, b, w->q, w->n);
+  return BRI17_OK;
+}
+
+static int solve_plain64(bri17_op* op, const double* b, double* x, double tol,
+                         int maxit, bri17_cg_info* info) {
+  CgWork* w;
+  int rc = ensure_work(op, false, &w);
+  if (rc != BRI17_OK) return rc;
+  const int64_t n = w->n;
+  cudaStream_t s = w->stream;
+  const int rb = red_blocks(n);
+  BRI17_CUDA_TRY(cudaMemcpyAsync(w->x, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  const double bb = w->st_host->aux;
+  if (!isfinite(bb)) {
+    set_error("right-hand side is not finite");
+    info->status = BRI17_ERR_BREAKDOWN;
+    return BRI17_ERR_BREAKDOWN;
+  }
+  if (!(bb > 0.0)) {
+    // b = 0: the mean-free solution is x = 0.
+    BRI17_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+    BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+    info->iterations = 0;
+    info->outer_iterations = 1;
+    info->rel_residual = 0.0;
+    info->status = BRI17_OK;
+    return BRI17_OK;
+  }
+  rc = residual64(op, w, b);
+  if (rc != BRI17_OK) return rc;
+  // aux must hold b.b for k_start's threshold.
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+  k_start<double><<<rb, kRedThreads, 0, s>>>(w->r, w->p, n, w->st, w->partials, tol * tol);
+  int iters = 0;
+  int status = run_cg<double>(op, w, w->x, w->r, w->p, w->q, &w->graph64,
+                              &w->epoch64, maxit, &iters);
+  if (status == BRI17_ERR_CUDA || status == BRI17_ERR_OUT_OF_MEMORY) return status;
+  project_mean(op, w, w->x);
+  rc = residual64(op, w, b);
+  if (rc != BRI17_OK) return rc;
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(w->r, w->r, n, w->st, w->partials);
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  info->iterations = iters;
+  info->outer_iterations = 1;
+  info->rel_residual = sqrt(w->st_host->aux / bb);
+  if (status == BRI17_OK && !(info->rel_residual <= tol * 1.0000001 + 1e-300)) {
+    // The recursive residual met tol but the recomputed one did not.
+    status = BRI17_ERR_NOT_CONVERGED;
+  }
+  info->status = status;
+  BRI17_CUDA_TRY(cudaMemcpyAsync(x, w->x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+  return status;
+}
+
+__global__ void k_residual_f32(float* __restrict__ r, const double* __restrict__ b,
+                               const float* __restrict__ kx, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = (float)(b[i] - (double)kx[i]);
+}
+
+__global__ void k_f64_to_f32(float* out, const double* in, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// Plain CG on an FP32 handle: FP32 vectors and operator; b and x are FP64
+// at the interface.
+static int solve_plain32(bri17_op* op, const double* b, double* x, double tol,
+                         int maxit, bri17_cg_info* info) {
+  CgWork* w;
+  int rc = ensure_work(op, false, &w);
+  if (rc != BRI17_OK) return rc;
+  const int64_t n = w->n;
+  cudaStream_t s = w->stream;
+  const int rb = red_blocks(n);
+  k_f64_to_f32<<<grid1(n), 256, 0, s>>>(w->d32, x, n);
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  const double bb = w->st_host->aux;
+  if (!isfinite(bb)) {
+    set_error("right-hand side is not finite");
+    return BRI17_ERR_BREAKDOWN;
+  }
+  rc = apply_stiffness_async(op, w->d32, w->q32, s);
+  if (rc != BRI17_OK) return rc;
+  // r32 = b - K x32 (the product taken in FP32).
+  k_residual_f32<<<grid1(n), 256, 0, s>>>(w->r32, b, w->q32, n);
+  // aux = b.b for the stopping threshold.
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+  k_start<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->p32, n, w->st, w->partials, tol * tol);
+  int iters = 0;
+  int status = run_cg<float>(op, w, w->d32, w->r32, w->p32, w->q32, &w->graph32,
+                             &w->epoch32, maxit, &iters);
+  if (status == BRI17_ERR_CUDA || status == BRI17_ERR_OUT_OF_MEMORY) return status;
+  BRI17_CUDA_TRY(cudaMemsetAsync(w->x, 0, n * sizeof(double), s));
+  k_add_f32<<<grid1(n), 256, 0, s>>>(w->x, w->d32, 1.0, n);
+  project_mean(op, w, w->x);
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  info->iterations = iters;
+  info->outer_iterations = 1;
+  info->rel_residual = bb > 0 ? sqrt(w->st_host->rr / bb) : 0.0;
+  info->status = status;
+  BRI17_CUDA_TRY(cudaMemcpyAsync(x, w->x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+  return status;
+}
+
+// Mixed precision: FP64 outer refinement around an FP32 CG.
+static int solve_mixed(bri17_op* op, const double* b, double* x, double tol,
+                       int maxit, bri17_cg_info* info) {
+  if (op->precision != BRI17_F64) {
+    set_error("mixed-precision CG needs an FP64 handle");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  if (!op->twin32) {
+    int shape[3] = {op->g.n[0], op->g.n[1], op->g.n[2]};
+    int rc = bri17_op_create(op->g.dim, shape, op->L, op->mu, op->nu, BRI17_F32,
+                             &op->twin32);
+    if (rc != BRI17_OK) return rc;
+  }
+  bri17_op* op32 = op->twin32;
+  CgWork* w;
+  int rc = ensure_work(op, true, &w);
+  if (rc != BRI17_OK) return rc;
+  const int64_t n = w->n;
+  cudaStream_t s = w->stream;
+  const int rb = red_blocks(n);
+  BRI17_CUDA_TRY(cudaMemcpyAsync(w->x, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  const double bb = w->st_host->aux;
+  info->iterations = 0;
+  info->outer_iterations = 0;
+  if (!isfinite(bb)) {
+    set_error("right-hand side is not finite");
+    return BRI17_ERR_BREAKDOWN;
+  }
+  if (!(bb > 0.0)) {
+    BRI17_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+    BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+    info->rel_residual = 0.0;
+    info->status = BRI17_OK;
+    return BRI17_OK;
+  }
+  int status = BRI17_ERR_NOT_CONVERGED;
+  int total = 0;
+  double rel = 1.0;
+  const int max_outer = 40;
+  for (int outer = 0; outer <= max_outer; outer++) {
+    project_mean(op, w, w->x);
+    rc = residual64(op, w, b);
+    if (rc != BRI17_OK) return rc;
+    project_mean(op, w, w->r);
+    k_dot<double><<<rb, kRedThreads, 0, s>>>(w->r, w->r, n, w->st, w->partials);
+    rc = read_state(w);
+    if (rc != BRI17_OK) return rc;
+    const double rr = w->st_host->aux;
+    if (!isfinite(rr)) {
+      status = BRI17_ERR_BREAKDOWN;
+      break;
+    }
+    rel = sqrt(rr / bb);
+    if (rel <= tol) {
+      status = BRI17_OK;
+      break;
+    }
+    if (total >= maxit || outer == max_outer) {
+      status = BRI17_ERR_NOT_CONVERGED;
+      break;
+    }
+    info->outer_iterations = outer + 1;
+    // Inner: K d = r / ||r|| in FP32, to a relative residual that gains
+    // what is still needed (at most 1e-5, what FP32 resolves reliably).
+    double tin = 0.1 * tol / rel;
+    if (tin < 1e-5) tin = 1e-5;
+    if (tin > 1e-2) tin = 1e-2;
+    const double nr = sqrt(rr);
+    k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0 / nr, n);
+    BRI17_CUDA_TRY(cudaMemsetAsync(w->d32, 0, n * sizeof(float), s));
+    k_dot<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->r32, n, w->st, w->partials);
+    k_start<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->p32, n, w->st, w->partials,
+                                             tin * tin);
+    int iters = 0;
+    int st = run_cg<float>(op32, w, w->d32, w->r32, w->p32, w->q32, &w->graph32,
+                           &w->epoch32, maxit - total, &iters);
+    total += iters;
+    if (st == BRI17_ERR_CUDA || st == BRI17_ERR_OUT_OF_MEMORY) return st;
+    if (st == BRI17_ERR_BREAKDOWN && iters == 0) {
+      status = BRI17_ERR_BREAKDOWN;
+      break;
+    }
+    k_add_f32<<<grid1(n), 256, 0, s>>>(w->x, w->d32, nr, n);
+  }
+  info->iterations = total;
+  info->rel_residual = rel;
+  info->status = status;
+  BRI17_CUDA_TRY(cudaMemcpyAsync(x, w->x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+  return status;
+}
+
+}  // namespace bri17gb
+
+using namespace bri17gb;
+
+extern "C" int bri17_cg_solve(bri17_op* op, const double* b, double* x,
+                              double tol, int max_iterations, int mode,
+                              bri17_cg_info* info, void* stream) {
+  bri17_cg_info dummy;
+  if (!info) info = &dummy;
+  memset(info, 0, sizeof(*info));
+  if (!op || !b || !x) {
+    set_error("null pointer");
+    return info->status = BRI17_ERR_INVALID_ARGUMENT;
+  }
+  if (!(tol > 0) || max_iterations < 0 || (mode != BRI17_CG_PLAIN && mode != BRI17_CG_MIXED)) {
+    set_error("tol must be > 0, max_iterations >= 0, mode PLAIN or MIXED");
+    return info->status = BRI17_ERR_INVALID_ARGUMENT;
+  }
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return info->status = cuda_fail(e, "cudaStreamSynchronize");
+  int rc;
+  if (mode == BRI17_CG_MIXED)
+    rc = solve_mixed(op, b, x, tol, max_iterations, info);
+  else if (op->precision == BRI17_F64)
+    rc = solve_plain64(op, b, x, tol, max_iterations, info);
+  else
+    rc = solve_plain32(op, b, x, tol, max_iterations, info);
+  info->status = rc;
+  return rc;
+}

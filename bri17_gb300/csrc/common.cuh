@@ -1,0 +1,56 @@
+// common.cuh -- shared host/device declarations of the bri17 GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/bri17_gb300.h"
+#include "fft.cuh"
+
+namespace bri17gb {
+
+// Per-thread last-error text behind bri17_last_error().
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define BRI17_CUDA_TRY(expr)                           \
+  do {                                                 \
+    cudaError_t _e = (expr);                           \
+    if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
+  } while (0)
+
+// Device tables of one operator, in scalar type T.  For axis i of length n:
+//   tw[i][t]   = exp(-2 pi i t / n), t in [0, n)           (FFT twiddles)
+//   kphi/kchi/kpsi[i][k] = phi, chi, psi of Hooke::modal_stiffness
+//                (include/bri17/bri17.hpp:258-264), k in [0, n)
+//   bc[i][k] = cos(alpha), bs[i][k] = sin(alpha) N / L, ea[i][k] =
+//                (cos alpha, sin alpha), alpha = pi k / N, the factors of
+//                Hooke::modal_strain_displacement (:217-224)
+template <typename T>
+struct Tables {
+  const cplx<T>* tw[3];
+  const T* kphi[3];
+  const T* kchi[3];
+  const T* kpsi[3];
+  const T* bc[3];
+  const T* bs[3];
+  const cplx<T>* ea[3];
+};
+
+// Geometry of one operator's real fields and half spectrum.
+struct Geometry {
+  int dim;
+  int n[3];        // cells per axis (axis dim-1 is the contiguous one)
+  int H;           // n[dim-1] / 2 + 1
+  int64_t size;    // nodes
+  int64_t P;       // spectrum lines per component along axis 0
+  int64_t cspec;   // complex spectrum entries per component (n[0] * P)
+  AxisPlan plan_row;  // last axis: length n/2 (even n) or n (odd n)
+  AxisPlan plan[3];   // full-length plans of each axis
+};
+
+bool make_plan(int n, AxisPlan* p);
+
+}  // namespace bri17gb

@@ -1,0 +1,58 @@
+// op.cuh -- the operator handle shared by the library's translation units.
+#pragma once
+
+#include "common.cuh"
+
+struct bri17_op {
+  bri17gb::Geometry g;
+  double L[3];
+  double mu;
+  double nu;
+  int precision;  // bri17_precision
+  int device;
+  double cell_volume;  // |h|, accumulated like tests/test_bri17.cpp:93-97
+  double corr;         // |h| / |N|, tests/test_bri17.cpp:98
+
+  void* table_mem;                 // one device allocation for all tables
+  bri17gb::Tables<double> tab64;   // always present (per-mode batch API)
+  bri17gb::Tables<float> tab32;    // F32 handles only
+
+  void* spec;          // half spectrum, spec_comps * g.cspec complex
+  int spec_comps;
+  void* stage_in;      // host-API staging buffers (lazy)
+  void* stage_out;
+  size_t stage_bytes;
+
+  // Conjugate-gradient work space (lazy, owned by cg.cu).
+  void* cg_work;
+  void (*cg_free)(void*);
+  bri17_op* twin32;    // FP32 twin of an FP64 handle for mixed-precision CG
+  unsigned material_epoch;  // bumped by bri17_op_set_material
+  void* timing;             // PassTiming while per-pass timing is enabled
+};
+
+namespace bri17gb {
+
+// Scalar byte size of a handle's fields.
+inline size_t scalar_bytes(const bri17_op* op) {
+  return op->precision == BRI17_F64 ? sizeof(double) : sizeof(float);
+}
+
+// Grow the spectrum buffer to `comps` components.
+int ensure_spectrum(bri17_op* op, int comps);
+
+// Enqueue f = K u on `stream` for a handle of either precision.
+int apply_stiffness_async(bri17_op* op, const void* u, void* f,
+                          cudaStream_t stream);
+
+// Batched forms used by the server: `batch` fields of one geometry,
+// contiguous (entry z at z * dim * size), with per-entry material
+// (s, mu) pairs in `mat` (device, precision of the handle, already scaled by
+// |h|/|N|).  spec must hold batch * dim * cspec complex values.
+int apply_stiffness_batched_async(bri17_op* op, int batch, const void* u,
+                                  void* f, void* spec, const void* mat,
+                                  cudaStream_t stream);
+int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
+                                  void* b, void* spec, cudaStream_t stream);
+
+}  // namespace bri17gb

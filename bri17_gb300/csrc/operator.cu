@@ -1,0 +1,955 @@
+// operator.cu -- operator handle, FFT plans, per-mode batch kernels and the
+// C ABI of the periodic stiffness operator (include/bri17_gb300.h).
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "op.cuh"
+#include "passes.cuh"
+
+namespace bri17gb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? BRI17_ERR_OUT_OF_MEMORY
+                                        : BRI17_ERR_CUDA;
+}
+
+static int invalid(const char* msg) {
+  set_error(msg);
+  return BRI17_ERR_INVALID_ARGUMENT;
+}
+
+// ---------------------------------------------------------------------------
+// Plans.
+
+bool make_plan(int n, AxisPlan* p) {
+  memset(p, 0, sizeof(*p));
+  p->n = n;
+  if (n < 1) return false;
+  int e = 0, m = n;
+  while (m % 2 == 0) {
+    m /= 2;
+    e++;
+  }
+  std::vector<int> r;
+  const int q = e / 4, rem = e % 4;
+  for (int i = 0; i < q; i++) r.push_back(16);
+  if (rem == 1) {
+    if (q >= 1) {
+      r.pop_back();
+      r.push_back(8);
+      r.push_back(4);
+    } else {
+      r.push_back(2);
+    }
+  } else if (rem == 2) {
+    r.push_back(4);
+  } else if (rem == 3) {
+    r.push_back(8);
+  }
+  for (int f = 3; m > 1; f += 2) {
+    while (m % f == 0) {
+      if (f > kMaxGenericRadix) return false;
+      r.push_back(f);
+      m /= f;
+    }
+  }
+  if ((int)r.size() > kMaxStages) return false;
+  p->nstages = (int)r.size();
+  for (int i = 0; i < p->nstages; i++) p->radix[i] = r[i];
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Tables.  Twiddles are computed in long double with an exact argument and
+// rounded once; the modal factors repeat the reference's double expressions
+// (include/bri17/bri17.hpp:217-222, :258-264) so that the per-mode API is
+// bit-identical to it.
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+struct HostTables {
+  std::vector<double> twr, twi, kphi, kchi, kpsi, bc, bs, ec, es;
+};
+
+static void host_tables(int n, double L, HostTables* t) {
+  const long double pil = 3.141592653589793238462643383279502884L;
+  t->twr.resize(n);
+  t->twi.resize(n);
+  t->kphi.resize(n);
+  t->kchi.resize(n);
+  t->kpsi.resize(n);
+  t->bc.resize(n);
+  t->bs.resize(n);
+  t->ec.resize(n);
+  t->es.resize(n);
+  for (int k = 0; k < n; k++) {
+    const long double ang = 2.0L * pil * (long double)k / (long double)n;
+    t->twr[k] = (double)cosl(ang);
+    t->twi[k] = (double)-sinl(ang);
+    const double h = L / n;
+    const double beta = 2 * kPi * k / n;
+    t->kphi[k] = 2 * (1 - cos(beta)) / h / h;
+    t->kchi[k] = (2 + cos(beta)) / 3;
+    t->kpsi[k] = sin(beta) / h;
+    const double alpha = kPi * k / n;
+    t->bc[k] = cos(alpha);
+    t->bs[k] = sin(alpha) * n / L;
+    t->ec[k] = cos(alpha);
+    t->es[k] = sin(alpha);
+  }
+}
+
+static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+template <typename T>
+static void fill_tables(const std::vector<HostTables>& ht, const int* n,
+                        int dim, unsigned char* host, size_t* off,
+                        Tables<T>* tab, unsigned char* dev) {
+  for (int i = 0; i < 3; i++) {
+    tab->tw[i] = nullptr;
+    tab->kphi[i] = tab->kchi[i] = tab->kpsi[i] = tab->bc[i] = tab->bs[i] =
+        nullptr;
+    tab->ea[i] = nullptr;
+  }
+  for (int i = 0; i < dim; i++) {
+    const HostTables& t = ht[i];
+    const int m = n[i];
+    // twiddles
+    {
+      cplx<T>* h = reinterpret_cast<cplx<T>*>(host + *off);
+      for (int k = 0; k < m; k++) {
+        h[k].x = (T)t.twr[k];
+        h[k].y = (T)t.twi[k];
+      }
+      tab->tw[i] = reinterpret_cast<const cplx<T>*>(dev + *off);
+      *off = align16(*off + m * sizeof(cplx<T>));
+    }
+    {
+      cplx<T>* h = reinterpret_cast<cplx<T>*>(host + *off);
+      for (int k = 0; k < m; k++) {
+        h[k].x = (T)t.ec[k];
+        h[k].y = (T)t.es[k];
+      }
+      tab->ea[i] = reinterpret_cast<const cplx<T>*>(dev + *off);
+      *off = align16(*off + m * sizeof(cplx<T>));
+    }
+    const std::vector<double>* src[5] = {&t.kphi, &t.kchi, &t.kpsi, &t.bc,
+                                         &t.bs};
+    const T** dst[5] = {&tab->kphi[i], &tab->kchi[i], &tab->kpsi[i],
+                        &tab->bc[i], &tab->bs[i]};
+    for (int j = 0; j < 5; j++) {
+      T* h = reinterpret_cast<T*>(host + *off);
+      for (int k = 0; k < m; k++) h[k] = (T)(*src[j])[k];
+      *dst[j] = reinterpret_cast<const T*>(dev + *off);
+      *off = align16(*off + m * sizeof(T));
+    }
+  }
+}
+
+static size_t tables_bytes(const int* n, int dim, size_t tsize) {
+  size_t b = 0;
+  for (int i = 0; i < dim; i++) {
+    b = align16(b + n[i] * 2 * tsize);
+    b = align16(b + n[i] * 2 * tsize);
+    for (int j = 0; j < 5; j++) b = align16(b + n[i] * tsize);
+  }
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Launch helpers.
+
+constexpr int kTileElems = 2048;        // complex values per CTA tile
+constexpr size_t kFusedSmemBudget = 100 * 1024;
+constexpr size_t kMaxSmem = 227 * 1024;
+
+template <typename T>
+static void set_smem_attrs() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(rows_r2c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(rows_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis_c2c<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis_c2c<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+#define SET_FUSED(D, M) \
+  cudaFuncSetAttribute(axis0_fused<T, D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem)
+    SET_FUSED(2, kModeStiffness);
+    SET_FUSED(3, kModeStiffness);
+    SET_FUSED(2, kModeStrain);
+    SET_FUSED(3, kModeStrain);
+    SET_FUSED(2, kModeRhs);
+    SET_FUSED(3, kModeRhs);
+#undef SET_FUSED
+    cudaGetLastError();
+  });
+}
+
+template <typename T>
+static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
+                           int64_t nrows, const Tables<T>& tab,
+                           cudaStream_t st) {
+  const int n = g.n[g.dim - 1];
+  const int m = (n % 2 == 0) ? n / 2 : n;
+  const int pitch = m + 1;
+  int rows = (int)std::max<int64_t>(1, std::min<int64_t>(nrows, kTileElems / m));
+  size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)rows * pitch * sizeof(cplx<T>);
+  const int64_t grid = (nrows + rows - 1) / rows;
+  rows_r2c<T><<<(unsigned)grid, kThreads, smem, st>>>(x, X, nrows, n, g.H, g.plan_row,
+                                                      tab.tw[g.dim - 1], rows, pitch);
+  return BRI17_OK;
+}
+
+template <typename T>
+static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
+                           int64_t nrows, const Tables<T>& tab,
+                           cudaStream_t st) {
+  const int n = g.n[g.dim - 1];
+  const int m = (n % 2 == 0) ? n / 2 : n;
+  const int pitch = m + 1;
+  int rows = (int)std::max<int64_t>(1, std::min<int64_t>(nrows, kTileElems / m));
+  size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)rows * pitch * sizeof(cplx<T>);
+  const int64_t grid = (nrows + rows - 1) / rows;
+  rows_c2r<T><<<(unsigned)grid, kThreads, smem, st>>>(X, x, nrows, n, g.H, g.plan_row,
+                                                      tab.tw[g.dim - 1], rows, pitch);
+  return BRI17_OK;
+}
+
+template <typename T, bool INV>
+static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
+                        const Tables<T>& tab, cudaStream_t st) {
+  const int n = g.n[1];
+  const int64_t B = g.H;
+  const int pitch = n + 1;
+  int TB = (int)std::min<int64_t>(B, std::max(4, std::min(32, kTileElems / n)));
+  size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)TB * pitch * sizeof(cplx<T>);
+  dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);
+  axis_c2c<T, INV><<<grid, kThreads, smem, st>>>(X, n, B, TB, pitch, g.plan[1], tab.tw[1]);
+  return BRI17_OK;
+}
+
+template <typename T, int DIM, int MODE>
+static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
+                        int64_t bstride, const FusedParams<T>& fp,
+                        cudaStream_t st) {
+  constexpr int SYM = DIM == 2 ? 3 : 6;
+  constexpr int CIN = MODE == kModeRhs ? SYM : DIM;
+  constexpr int COUT = MODE == kModeStrain ? SYM : DIM;
+  constexpr int CMAX = CIN > COUT ? CIN : COUT;
+  const int n0 = g.n[0];
+  const int pitch = n0 + 1;
+  const size_t per_line = (size_t)(CMAX + 1) * pitch * sizeof(cplx<T>);
+  size_t budget = kFusedSmemBudget;
+  int TB = (int)std::min<size_t>(16, budget / per_line);
+  if (TB < 4) {
+    budget = kMaxSmem - n0 * sizeof(cplx<T>) - 1024;
+    TB = (int)std::min<size_t>(4, budget / per_line);
+  }
+  if (TB < 1) {
+    set_error("axis-0 tile does not fit in shared memory");
+    return BRI17_ERR_UNSUPPORTED_SIZE;
+  }
+  TB = (int)std::min<int64_t>(TB, g.P);
+  size_t smem = n0 * sizeof(cplx<T>) + (size_t)TB * per_line;
+  dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
+  axis0_fused<T, DIM, MODE><<<grid, kThreads, smem, st>>>(
+      X, n0, g.P, g.cspec, bstride, TB, pitch, g.plan[0], fp);
+  return BRI17_OK;
+}
+
+template <typename T>
+static FusedParams<T> fused_params(const bri17_op* op, const Tables<T>& tab,
+                                   int mode) {
+  FusedParams<T> fp;
+  fp.tab = tab;
+  fp.n1 = op->g.dim == 3 ? op->g.n[1] : 1;
+  fp.H = op->g.H;
+  const double scaling = op->mu / (1. - 2. * op->nu);
+  fp.s = (T)(scaling * op->corr);
+  fp.mu = (T)(op->mu * op->corr);
+  fp.corr = mode == kModeStrain ? (T)(1.0 / (double)op->g.size) : (T)op->corr;
+  fp.mat = nullptr;
+  return fp;
+}
+
+// ---------------------------------------------------------------------------
+// Per-pass timing.
+
+constexpr int kNumPasses = 5;
+
+struct PassTiming {
+  struct Rec {
+    int pass;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Rec> recs;
+  double ms[kNumPasses] = {0, 0, 0, 0, 0};
+  int64_t n[kNumPasses] = {0, 0, 0, 0, 0};
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void harvest() {
+    for (auto& r : recs) {
+      float t = 0.f;
+      cudaEventSynchronize(r.b);
+      if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+        ms[r.pass] += t;
+        n[r.pass] += 1;
+      }
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    recs.clear();
+  }
+  ~PassTiming() {
+    harvest();
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+// Brackets one launch with events when timing is enabled.
+struct PassScope {
+  PassTiming* t;
+  PassTiming::Rec rec;
+  cudaStream_t st;
+  PassScope(bri17_op* op, int pass, cudaStream_t s)
+      : t(reinterpret_cast<PassTiming*>(op->timing)), st(s) {
+    if (!t) return;
+    rec.pass = pass;
+    rec.a = t->get();
+    rec.b = t->get();
+    cudaEventRecord(rec.a, st);
+  }
+  ~PassScope() {
+    if (!t) return;
+    cudaEventRecord(rec.b, st);
+    t->recs.push_back(rec);
+  }
+};
+
+// Generic three- or five-pass pipeline: forward rows (+ axis 1), fused axis
+// 0, inverse axis 1 (+ rows).  `in` has cin components, `out` cout.
+template <typename T, int MODE>
+static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
+                        T* out, int batch, void* spec, const T* mat,
+                        cudaStream_t st) {
+  const Geometry& g = op->g;
+  const int dim = g.dim;
+  const int sym = dim == 2 ? 3 : 6;
+  const int cin = MODE == kModeRhs ? sym : dim;
+  const int cout = MODE == kModeStrain ? sym : dim;
+  const int cmax = cin > cout ? cin : cout;
+  const int nlast = g.n[dim - 1];
+  const int64_t rows_per_comp = g.size / nlast;
+  cplx<T>* S = reinterpret_cast<cplx<T>*>(spec);
+  const int64_t bstride = (int64_t)cmax * g.cspec;
+  set_smem_attrs<T>();
+  // Forward rows / axis 1, per batch entry (components contiguous).
+  for (int z = 0; z < batch; z++) {
+    const T* src = in + (int64_t)z * cin * g.size;
+    cplx<T>* Sz = S + z * bstride;
+    {
+      PassScope ps(op, 0, st);
+      launch_rows_r2c<T>(g, src, Sz, cin * rows_per_comp, tab, st);
+    }
+    if (dim == 3) {
+      PassScope ps(op, 1, st);
+      launch_axis1<T, false>(g, Sz, (int64_t)cin * g.n[0], tab, st);
+    }
+  }
+  FusedParams<T> fp = fused_params<T>(op, tab, MODE);
+  fp.mat = mat;
+  int rc;
+  {
+    PassScope ps(op, 2, st);
+    if (dim == 3)
+      rc = launch_fused<T, 3, MODE>(g, S, batch, bstride, fp, st);
+    else
+      rc = launch_fused<T, 2, MODE>(g, S, batch, bstride, fp, st);
+  }
+  if (rc != BRI17_OK) return rc;
+  for (int z = 0; z < batch; z++) {
+    T* dst = out + (int64_t)z * cout * g.size;
+    cplx<T>* Sz = S + z * bstride;
+    if (dim == 3) {
+      PassScope ps(op, 3, st);
+      launch_axis1<T, true>(g, Sz, (int64_t)cout * g.n[0], tab, st);
+    }
+    {
+      PassScope ps(op, 4, st);
+      launch_rows_c2r<T>(g, Sz, dst, cout * rows_per_comp, tab, st);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "operator launch");
+  return BRI17_OK;
+}
+
+int ensure_spectrum(bri17_op* op, int comps) {
+  if (op->spec && op->spec_comps >= comps) return BRI17_OK;
+  const size_t csz = 2 * scalar_bytes(op);
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, (size_t)comps * op->g.cspec * csz);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(spectrum)");
+  if (op->spec) {
+    cudaDeviceSynchronize();
+    cudaFree(op->spec);
+  }
+  op->spec = p;
+  op->spec_comps = comps;
+  return BRI17_OK;
+}
+
+int apply_stiffness_async(bri17_op* op, const void* u, void* f,
+                          cudaStream_t st) {
+  int rc = ensure_spectrum(op, op->g.dim);
+  if (rc != BRI17_OK) return rc;
+  if (op->precision == BRI17_F64)
+    return run_pipeline<double, kModeStiffness>(
+        op, op->tab64, (const double*)u, (double*)f, 1, op->spec, nullptr, st);
+  return run_pipeline<float, kModeStiffness>(
+      op, op->tab32, (const float*)u, (float*)f, 1, op->spec, nullptr, st);
+}
+
+int apply_stiffness_batched_async(bri17_op* op, int batch, const void* u,
+                                  void* f, void* spec, const void* mat,
+                                  cudaStream_t st) {
+  if (op->precision == BRI17_F64)
+    return run_pipeline<double, kModeStiffness>(op, op->tab64, (const double*)u,
+                                                (double*)f, batch, spec,
+                                                (const double*)mat, st);
+  return run_pipeline<float, kModeStiffness>(op, op->tab32, (const float*)u,
+                                             (float*)f, batch, spec,
+                                             (const float*)mat, st);
+}
+
+int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
+                                  void* b, void* spec, cudaStream_t st) {
+  if (op->precision == BRI17_F64)
+    return run_pipeline<double, kModeRhs>(op, op->tab64, (const double*)tau,
+                                          (double*)b, batch, spec, nullptr, st);
+  return run_pipeline<float, kModeRhs>(op, op->tab32, (const float*)tau,
+                                       (float*)b, batch, spec, nullptr, st);
+}
+
+// ---------------------------------------------------------------------------
+// Per-mode batch kernels (FP64).  Operation order and rounding follow the
+// reference line by line; __dmul_rn / __dadd_rn keep the compiler from
+// contracting products into fused multiply-adds the reference does not do.
+
+struct ModalArgs {
+  Tables<double> tab;
+  int dim;
+  int n[3];
+  double scaling;  // mu / (1 - 2 nu), include/bri17/bri17.hpp:266
+  double mu;
+};
+
+__device__ __forceinline__ int wrap(int k, int n) {
+  int r = k % n;
+  return r < 0 ? r + n : r;
+}
+
+// Hooke::modal_stiffness, include/bri17/bri17.hpp:247-292 (real parts).
+__device__ void modal_stiffness_dev(const ModalArgs& a, const int* kk,
+                                    double* K) {
+  double phi[3], chi[3], psi[3];
+  for (int i = 0; i < a.dim; i++) {
+    phi[i] = a.tab.kphi[i][kk[i]];
+    chi[i] = a.tab.kchi[i][kk[i]];
+    psi[i] = a.tab.kpsi[i][kk[i]];
+  }
+  const double s = a.scaling;
+  if (a.dim == 2) {
+    const double H00 = __dmul_rn(phi[0], chi[1]);
+    const double H11 = __dmul_rn(chi[0], phi[1]);
+    const double Kd = __dmul_rn(a.mu, __dadd_rn(H00, H11));
+    K[0] = __dadd_rn(__dmul_rn(s, H00), Kd);
+    K[1] = __dmul_rn(__dmul_rn(s, psi[0]), psi[1]);
+    K[2] = K[1];
+    K[3] = __dadd_rn(__dmul_rn(s, H11), Kd);
+  } else {
+    const double H00 = __dmul_rn(__dmul_rn(phi[0], chi[1]), chi[2]);
+    const double H11 = __dmul_rn(__dmul_rn(chi[0], phi[1]), chi[2]);
+    const double H22 = __dmul_rn(__dmul_rn(chi[0], chi[1]), phi[2]);
+    const double Kd = __dmul_rn(a.mu, __dadd_rn(__dadd_rn(H00, H11), H22));
+    K[0] = __dadd_rn(__dmul_rn(s, H00), Kd);
+    K[1] = __dmul_rn(__dmul_rn(__dmul_rn(s, psi[0]), psi[1]), chi[2]);
+    K[2] = __dmul_rn(__dmul_rn(__dmul_rn(s, psi[0]), chi[1]), psi[2]);
+    K[3] = K[1];
+    K[4] = __dadd_rn(__dmul_rn(s, H11), Kd);
+    K[5] = __dmul_rn(__dmul_rn(__dmul_rn(s, chi[0]), psi[1]), psi[2]);
+    K[6] = K[2];
+    K[7] = K[5];
+    K[8] = __dadd_rn(__dmul_rn(s, H22), Kd);
+  }
+}
+
+// Hooke::modal_strain_displacement, include/bri17/bri17.hpp:212-236.
+__device__ void modal_strain_displacement_dev(const ModalArgs& a,
+                                              const int* kk, double2* B) {
+  double c[3], s[3];
+  double sum_alpha = 0.0;
+  for (int i = 0; i < a.dim; i++) {
+    const double alpha = __ddiv_rn(__dmul_rn(kPi, (double)kk[i]), (double)a.n[i]);
+    sum_alpha = __dadd_rn(sum_alpha, alpha);
+    c[i] = a.tab.bc[i][kk[i]];
+    s[i] = a.tab.bs[i][kk[i]];
+  }
+  double sn, cs;
+  sincos(sum_alpha, &sn, &cs);
+  const double pr = -2 * sn, pi = 2 * cs;
+  if (a.dim == 2) {
+    B[0] = make_double2(__dmul_rn(__dmul_rn(pr, s[0]), c[1]),
+                        __dmul_rn(__dmul_rn(pi, s[0]), c[1]));
+    B[1] = make_double2(__dmul_rn(__dmul_rn(pr, c[0]), s[1]),
+                        __dmul_rn(__dmul_rn(pi, c[0]), s[1]));
+  } else {
+    B[0] = make_double2(__dmul_rn(__dmul_rn(__dmul_rn(pr, s[0]), c[1]), c[2]),
+                        __dmul_rn(__dmul_rn(__dmul_rn(pi, s[0]), c[1]), c[2]));
+    B[1] = make_double2(__dmul_rn(__dmul_rn(__dmul_rn(pr, c[0]), s[1]), c[2]),
+                        __dmul_rn(__dmul_rn(__dmul_rn(pi, c[0]), s[1]), c[2]));
+    B[2] = make_double2(__dmul_rn(__dmul_rn(__dmul_rn(pr, c[0]), c[1]), s[2]),
+                        __dmul_rn(__dmul_rn(__dmul_rn(pi, c[0]), c[1]), s[2]));
+  }
+}
+
+__global__ void modal_stiffness_kernel(ModalArgs a, const int* __restrict__ k,
+                                       int64_t n, double2* __restrict__ K) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  int kk[3];
+  for (int i = 0; i < a.dim; i++) kk[i] = wrap(k[m * a.dim + i], a.n[i]);
+  double Kr[9];
+  modal_stiffness_dev(a, kk, Kr);
+  const int d2 = a.dim * a.dim;
+  for (int i = 0; i < d2; i++) K[m * d2 + i] = make_double2(Kr[i], 0.0);
+}
+
+__global__ void modal_strain_kernel(ModalArgs a, const int* __restrict__ k,
+                                    int64_t n, double2* __restrict__ B) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  int kk[3];
+  for (int i = 0; i < a.dim; i++) kk[i] = wrap(k[m * a.dim + i], a.n[i]);
+  double2 b[3];
+  modal_strain_displacement_dev(a, kk, b);
+  for (int i = 0; i < a.dim; i++) B[m * a.dim + i] = b[i];
+}
+
+// Hooke::modal_eigenstress_to_opposite_strain, include/bri17/bri17.hpp:
+// 308-355: solve K u = tau . conj(B) (K real SPD for k != 0, factored by a
+// real Cholesky), return sym(B (x) u) in Mandel form; k = 0 gives 0.
+__global__ void modal_eigenstress_kernel(ModalArgs a, const int* __restrict__ k,
+                                         int64_t n,
+                                         const double2* __restrict__ tau,
+                                         double2* __restrict__ eta) {
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int dim = a.dim;
+  const int sym = dim == 2 ? 3 : 6;
+  int kk[3];
+  bool null_frequency = true;
+  for (int i = 0; i < dim; i++) {
+    const int ki = k[m * dim + i];
+    kk[i] = wrap(ki, a.n[i]);
+    null_frequency = null_frequency && (ki == 0);
+  }
+  if (null_frequency) {
+    for (int q = 0; q < sym; q++) eta[m * sym + q] = make_double2(0.0, 0.0);
+    return;
+  }
+  double2 B[3];
+  double K[9];
+  modal_strain_displacement_dev(a, kk, B);
+  modal_stiffness_dev(a, kk, K);
+  const double ir2 = 0.7071067811865475244008443621048490392848;
+  const double r2 = 1.414213562373095048801688724209698079;
+  double2 t[3][3];
+  const double2* tm = tau + m * sym;
+  if (dim == 2) {
+    t[0][0] = tm[0];
+    t[1][1] = tm[1];
+    t[0][1] = t[1][0] = make_double2(tm[2].x * ir2, tm[2].y * ir2);
+  } else {
+    t[0][0] = tm[0];
+    t[1][1] = tm[1];
+    t[2][2] = tm[2];
+    t[1][2] = t[2][1] = make_double2(tm[3].x * ir2, tm[3].y * ir2);
+    t[0][2] = t[2][0] = make_double2(tm[4].x * ir2, tm[4].y * ir2);
+    t[0][1] = t[1][0] = make_double2(tm[5].x * ir2, tm[5].y * ir2);
+  }
+  double2 rhs[3];
+  for (int i = 0; i < dim; i++) {
+    double sr = 0.0, si = 0.0;
+    for (int j = 0; j < dim; j++) {
+      const double br = B[j].x, bi = -B[j].y;
+      sr += t[i][j].x * br - t[i][j].y * bi;
+      si += t[i][j].x * bi + t[i][j].y * br;
+    }
+    rhs[i] = make_double2(sr, si);
+  }
+  double Lc[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int j = 0; j < dim; j++) {
+    double d = K[j * dim + j];
+    for (int p = 0; p < j; p++) d -= Lc[j][p] * Lc[j][p];
+    d = sqrt(d);
+    Lc[j][j] = d;
+    for (int i = j + 1; i < dim; i++) {
+      double s = K[i * dim + j];
+      for (int p = 0; p < j; p++) s -= Lc[i][p] * Lc[j][p];
+      Lc[i][j] = s / d;
+    }
+  }
+  double2 y[3], u[3];
+  for (int i = 0; i < dim; i++) {
+    double sr = rhs[i].x, si = rhs[i].y;
+    for (int p = 0; p < i; p++) {
+      sr -= Lc[i][p] * y[p].x;
+      si -= Lc[i][p] * y[p].y;
+    }
+    y[i] = make_double2(sr / Lc[i][i], si / Lc[i][i]);
+  }
+  for (int i = dim - 1; i >= 0; i--) {
+    double sr = y[i].x, si = y[i].y;
+    for (int p = i + 1; p < dim; p++) {
+      sr -= Lc[p][i] * u[p].x;
+      si -= Lc[p][i] * u[p].y;
+    }
+    u[i] = make_double2(sr / Lc[i][i], si / Lc[i][i]);
+  }
+  static const int I3[6] = {0, 1, 2, 1, 2, 0}, J3[6] = {0, 1, 2, 2, 0, 1};
+  static const int I2[3] = {0, 1, 0}, J2[3] = {0, 1, 1};
+  for (int q = 0; q < sym; q++) {
+    const int i = dim == 2 ? I2[q] : I3[q];
+    const int j = dim == 2 ? J2[q] : J3[q];
+    double er = 0.5 * ((B[i].x * u[j].x - B[i].y * u[j].y) +
+                       (u[i].x * B[j].x - u[i].y * B[j].y));
+    double ei = 0.5 * ((B[i].x * u[j].y + B[i].y * u[j].x) +
+                       (u[i].x * B[j].y + u[i].y * B[j].x));
+    if (i != j) {
+      er *= r2;
+      ei *= r2;
+    }
+    eta[m * sym + q] = make_double2(er, ei);
+  }
+}
+
+static ModalArgs modal_args(const bri17_op* op) {
+  ModalArgs a;
+  a.tab = op->tab64;
+  a.dim = op->g.dim;
+  for (int i = 0; i < 3; i++) a.n[i] = op->g.n[i];
+  a.scaling = op->mu / (1. - 2. * op->nu);
+  a.mu = op->mu;
+  return a;
+}
+
+static int check_material(double mu, double nu) {
+  if (!(mu > 0) || !isfinite(mu)) return invalid("mu must be positive and finite");
+  if (!(nu > -1.0 && nu < 0.5)) return invalid("nu must lie in (-1, 0.5)");
+  return BRI17_OK;
+}
+
+}  // namespace bri17gb
+
+using namespace bri17gb;
+
+// ---------------------------------------------------------------------------
+// C ABI.
+
+extern "C" const char* bri17_status_string(int s) {
+  switch (s) {
+    case BRI17_OK: return "ok";
+    case BRI17_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case BRI17_ERR_UNSUPPORTED_SIZE: return "unsupported size";
+    case BRI17_ERR_CUDA: return "CUDA error";
+    case BRI17_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case BRI17_ERR_NOT_CONVERGED: return "not converged";
+    case BRI17_ERR_BREAKDOWN: return "breakdown (NaN/Inf or loss of positivity)";
+    case BRI17_ERR_NO_DEVICE: return "no CUDA device";
+    case BRI17_ERR_BUSY: return "busy";
+    case BRI17_ERR_NOT_FOUND: return "not found";
+    case BRI17_ERR_CANCELLED: return "cancelled";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char* bri17_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char* bri17_version(void) { return "0.1.0"; }
+
+extern "C" int bri17_op_create(int dim, const int* shape, const double* L,
+                               double mu, double nu, int precision,
+                               bri17_op** out) {
+  if (!out || !shape || !L) return invalid("null pointer");
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return invalid("dim must be 2 or 3");
+  if (precision != BRI17_F64 && precision != BRI17_F32)
+    return invalid("precision must be BRI17_F64 or BRI17_F32");
+  int rc = check_material(mu, nu);
+  if (rc != BRI17_OK) return rc;
+  for (int i = 0; i < dim; i++) {
+    if (shape[i] < 1) return invalid("shape entries must be >= 1");
+    if (!(L[i] > 0) || !isfinite(L[i])) return invalid("L entries must be positive");
+    if (shape[i] > 1024) {
+      set_error("axis length above 1024");
+      return BRI17_ERR_UNSUPPORTED_SIZE;
+    }
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device visible");
+    return BRI17_ERR_NO_DEVICE;
+  }
+  bri17_op* op = new bri17_op();
+  memset(op, 0, sizeof(*op));
+  Geometry& g = op->g;
+  g.dim = dim;
+  g.size = 1;
+  for (int i = 0; i < 3; i++) {
+    g.n[i] = i < dim ? shape[i] : 1;
+    op->L[i] = i < dim ? L[i] : 1.0;
+  }
+  for (int i = 0; i < dim; i++) g.size *= shape[i];
+  if (g.size > ((int64_t)1 << 31) - 1) {
+    delete op;
+    set_error("grid larger than 2^31 - 1 nodes (CartesianGrid::size is int)");
+    return BRI17_ERR_UNSUPPORTED_SIZE;
+  }
+  const int nl = g.n[dim - 1];
+  g.H = nl / 2 + 1;
+  g.P = dim == 3 ? (int64_t)g.n[1] * g.H : (int64_t)g.H;
+  g.cspec = (int64_t)g.n[0] * g.P;
+  bool ok = make_plan(nl % 2 == 0 ? nl / 2 : nl, &g.plan_row);
+  for (int i = 0; i < dim; i++) ok = ok && make_plan(g.n[i], &g.plan[i]);
+  if (!ok) {
+    delete op;
+    set_error("axis length has a prime factor above 61");
+    return BRI17_ERR_UNSUPPORTED_SIZE;
+  }
+  op->mu = mu;
+  op->nu = nu;
+  op->precision = precision;
+  cudaGetDevice(&op->device);
+  double cv = 1.0;
+  for (int i = 0; i < dim; i++) cv *= op->L[i] / g.n[i];
+  op->cell_volume = cv;
+  op->corr = cv / (double)g.size;
+
+  std::vector<HostTables> ht(dim);
+  for (int i = 0; i < dim; i++) host_tables(g.n[i], op->L[i], &ht[i]);
+  const size_t b64 = tables_bytes(g.n, dim, sizeof(double));
+  const size_t b32 = precision == BRI17_F32 ? tables_bytes(g.n, dim, sizeof(float)) : 0;
+  std::vector<unsigned char> host(b64 + b32 + 16);
+  cudaError_t e = cudaMalloc(&op->table_mem, b64 + b32 + 16);
+  if (e != cudaSuccess) {
+    delete op;
+    return cuda_fail(e, "cudaMalloc(tables)");
+  }
+  size_t off = 0;
+  unsigned char* dev = (unsigned char*)op->table_mem;
+  fill_tables<double>(ht, g.n, dim, host.data(), &off, &op->tab64, dev);
+  if (precision == BRI17_F32)
+    fill_tables<float>(ht, g.n, dim, host.data(), &off, &op->tab32, dev);
+  e = cudaMemcpy(op->table_mem, host.data(), off, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(op->table_mem);
+    delete op;
+    return cuda_fail(e, "cudaMemcpy(tables)");
+  }
+  rc = ensure_spectrum(op, dim);
+  if (rc != BRI17_OK) {
+    cudaFree(op->table_mem);
+    delete op;
+    return rc;
+  }
+  // Kernel attributes are set before any stream capture can begin.
+  if (precision == BRI17_F64)
+    set_smem_attrs<double>();
+  else
+    set_smem_attrs<float>();
+  *out = op;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_op_destroy(bri17_op* op) {
+  if (!op) return BRI17_OK;
+  cudaDeviceSynchronize();
+  if (op->twin32) bri17_op_destroy(op->twin32);
+  cudaFree(op->table_mem);
+  cudaFree(op->spec);
+  cudaFree(op->stage_in);
+  cudaFree(op->stage_out);
+  if (op->cg_work && op->cg_free) op->cg_free(op->cg_work);
+  delete reinterpret_cast<PassTiming*>(op->timing);
+  delete op;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_op_info(const bri17_op* op, int64_t* size,
+                             int64_t* workspace_bytes) {
+  if (!op) return invalid("null handle");
+  if (size) *size = op->g.size;
+  if (workspace_bytes)
+    *workspace_bytes = (int64_t)op->spec_comps * op->g.cspec * 2 * scalar_bytes(op);
+  return BRI17_OK;
+}
+
+extern "C" int bri17_op_set_material(bri17_op* op, double mu, double nu) {
+  if (!op) return invalid("null handle");
+  int rc = check_material(mu, nu);
+  if (rc != BRI17_OK) return rc;
+  op->mu = mu;
+  op->nu = nu;
+  op->material_epoch++;
+  if (op->twin32) bri17_op_set_material(op->twin32, mu, nu);
+  return BRI17_OK;
+}
+
+extern "C" int bri17_modal_stiffness_batch(const bri17_op* op, const int* k,
+                                           int64_t n, void* K, void* stream) {
+  if (!op) return invalid("null handle");
+  if (n < 0) return invalid("negative count");
+  if (n == 0) return BRI17_OK;
+  if (!k || !K) return invalid("null pointer");
+  ModalArgs a = modal_args(op);
+  modal_stiffness_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      a, k, n, (double2*)K);
+  BRI17_CUDA_TRY(cudaGetLastError());
+  return BRI17_OK;
+}
+
+extern "C" int bri17_modal_strain_displacement_batch(const bri17_op* op,
+                                                     const int* k, int64_t n,
+                                                     void* B, void* stream) {
+  if (!op) return invalid("null handle");
+  if (n < 0) return invalid("negative count");
+  if (n == 0) return BRI17_OK;
+  if (!k || !B) return invalid("null pointer");
+  ModalArgs a = modal_args(op);
+  modal_strain_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      a, k, n, (double2*)B);
+  BRI17_CUDA_TRY(cudaGetLastError());
+  return BRI17_OK;
+}
+
+extern "C" int bri17_modal_eigenstress_to_opposite_strain_batch(
+    const bri17_op* op, const int* k, int64_t n, const void* tau, void* eta,
+    void* stream) {
+  if (!op) return invalid("null handle");
+  if (n < 0) return invalid("negative count");
+  if (n == 0) return BRI17_OK;
+  if (!k || !tau || !eta) return invalid("null pointer");
+  ModalArgs a = modal_args(op);
+  modal_eigenstress_kernel<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      a, k, n, (const double2*)tau, (double2*)eta);
+  BRI17_CUDA_TRY(cudaGetLastError());
+  return BRI17_OK;
+}
+
+extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
+                                     void* stream) {
+  if (!op) return invalid("null handle");
+  if (!u || !f) return invalid("null pointer");
+  return apply_stiffness_async(op, u, f, (cudaStream_t)stream);
+}
+
+extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
+                                          void* f_host, void* stream) {
+  if (!op) return invalid("null handle");
+  if (!u_host || !f_host) return invalid("null pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = (size_t)op->g.dim * op->g.size * scalar_bytes(op);
+  if (op->stage_bytes < bytes) {
+    cudaFree(op->stage_in);
+    cudaFree(op->stage_out);
+    op->stage_in = op->stage_out = nullptr;
+    op->stage_bytes = 0;
+    BRI17_CUDA_TRY(cudaMalloc(&op->stage_in, bytes));
+    BRI17_CUDA_TRY(cudaMalloc(&op->stage_out, bytes));
+    op->stage_bytes = bytes;
+  }
+  BRI17_CUDA_TRY(cudaMemcpyAsync(op->stage_in, u_host, bytes, cudaMemcpyHostToDevice, st));
+  int rc = apply_stiffness_async(op, op->stage_in, op->stage_out, st);
+  if (rc != BRI17_OK) return rc;
+  BRI17_CUDA_TRY(cudaMemcpyAsync(f_host, op->stage_out, bytes, cudaMemcpyDeviceToHost, st));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(st));
+  return BRI17_OK;
+}
+
+extern "C" int bri17_apply_strain(bri17_op* op, const void* u, void* eps,
+                                  void* stream) {
+  if (!op) return invalid("null handle");
+  if (!u || !eps) return invalid("null pointer");
+  const int sym = op->g.dim == 2 ? 3 : 6;
+  int rc = ensure_spectrum(op, sym);
+  if (rc != BRI17_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (op->precision == BRI17_F64)
+    return run_pipeline<double, kModeStrain>(op, op->tab64, (const double*)u,
+                                             (double*)eps, 1, op->spec, nullptr, st);
+  return run_pipeline<float, kModeStrain>(op, op->tab32, (const float*)u,
+                                          (float*)eps, 1, op->spec, nullptr, st);
+}
+
+extern "C" int bri17_eigenstress_rhs(bri17_op* op, const void* tau, void* b,
+                                     void* stream) {
+  if (!op) return invalid("null handle");
+  if (!tau || !b) return invalid("null pointer");
+  const int sym = op->g.dim == 2 ? 3 : 6;
+  int rc = ensure_spectrum(op, sym);
+  if (rc != BRI17_OK) return rc;
+  return eigenstress_rhs_batched_async(op, 1, tau, b, op->spec, (cudaStream_t)stream);
+}
+
+extern "C" int bri17_op_set_pass_timing(bri17_op* op, int enable) {
+  if (!op) return invalid("null handle");
+  if (enable && !op->timing) op->timing = new PassTiming();
+  if (!enable && op->timing) {
+    delete reinterpret_cast<PassTiming*>(op->timing);
+    op->timing = nullptr;
+  }
+  return BRI17_OK;
+}
+
+extern "C" int bri17_op_pass_times(bri17_op* op, double* ms, int64_t* launches,
+                                   int max_passes, int* npasses) {
+  if (!op) return invalid("null handle");
+  PassTiming* t = reinterpret_cast<PassTiming*>(op->timing);
+  if (npasses) *npasses = kNumPasses;
+  if (!t) return invalid("pass timing is not enabled");
+  t->harvest();
+  for (int i = 0; i < kNumPasses && i < max_passes; i++) {
+    if (ms) ms[i] = t->ms[i];
+    if (launches) launches[i] = t->n[i];
+    t->ms[i] = 0;
+    t->n[i] = 0;
+  }
+  return BRI17_OK;
+}
+
+extern "C" const char* bri17_pass_name(int pass) {
+  static const char* names[kNumPasses] = {"rows_r2c", "axis_c2c_fwd", "axis0_fused",
+                                          "axis_c2c_inv", "rows_c2r"};
+  return pass >= 0 && pass < kNumPasses ? names[pass] : "unknown";
+}

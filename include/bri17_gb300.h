@@ -1,0 +1,261 @@
+/*
+ * bri17_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the bri17
+ * matrix-free periodic finite-element stiffness operator.
+ *
+ * The reference library (sbrisard/bri17) is a header-only C++ template pair,
+ * bri17::CartesianGrid<T,DIM> and bri17::Hooke<T,DIM>
+ * (include/bri17/bri17.hpp:34-356), whose per-mode functions the user
+ * combines with an FFT library; its only operator application is the test
+ * harness StiffnessMatrixFactory::compute_Ku (tests/test_bri17.cpp:56-107).
+ * This header exports, as plain C:
+ *
+ *   - an operator handle that owns one grid + one isotropic Hooke material
+ *     (the state of bri17::Hooke, include/bri17/bri17.hpp:176-194),
+ *   - batched forms of the per-mode functions Hooke::modal_stiffness and
+ *     Hooke::modal_strain_displacement (:212-292) and of
+ *     Hooke::modal_eigenstress_to_opposite_strain (:308-355),
+ *   - the whole-field operator f = K u that compute_Ku computes,
+ *   - the eigenstress right-hand side, the strain field u -> eps
+ *     (compute_Bu, tests/test_bri17.cpp:194-245), and conjugate-gradient
+ *     solvers of K u = b,
+ *   - a continuous-batching solve server.
+ *
+ * Conventions.
+ *   - Every function returns a status (bri17_status); none throws.
+ *   - Fields use the reference's layout: structure of arrays, component c of
+ *     node n at c * size + n, nodes row-major with the last axis fastest
+ *     (include/bri17/bri17.hpp:78-93, tests/test_bri17.cpp:66-67).
+ *   - Complex arrays are interleaved (re, im) pairs of the handle's scalar
+ *     type (double for BRI17_F64, float for BRI17_F32).
+ *   - "_dev" pointers are CUDA device pointers owned by the caller; work is
+ *     enqueued on `stream` (a cudaStream_t, NULL = legacy default stream) and
+ *     is stream-ordered: the call returns before the GPU finishes unless the
+ *     function says otherwise.  "_host" pointers are host memory; those
+ *     functions synchronise `stream` before returning.
+ *   - A handle is externally synchronised (one thread at a time); distinct
+ *     handles may be used concurrently.
+ */
+#ifndef BRI17_GB300_H_
+#define BRI17_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bri17_status {
+  BRI17_OK = 0,
+  BRI17_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad dim, nu >= 0.5, ... */
+  BRI17_ERR_UNSUPPORTED_SIZE = 2, /* an axis length the FFT plan rejects */
+  BRI17_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+  BRI17_ERR_OUT_OF_MEMORY = 4,    /* device allocation failed */
+  BRI17_ERR_NOT_CONVERGED = 5,    /* CG reached its iteration cap */
+  BRI17_ERR_BREAKDOWN = 6,        /* NaN/Inf or non-positive curvature */
+  BRI17_ERR_NO_DEVICE = 7,        /* no CUDA device visible */
+  BRI17_ERR_BUSY = 8,             /* server full / request slot taken */
+  BRI17_ERR_NOT_FOUND = 9,        /* unknown request id */
+  BRI17_ERR_CANCELLED = 10        /* request cancelled before it finished */
+} bri17_status;
+
+typedef enum bri17_precision {
+  BRI17_F64 = 0, /* FP64 FFT, FP64 modal matvec */
+  BRI17_F32 = 1  /* FP32 FFT, FP32 modal matvec */
+} bri17_precision;
+
+typedef struct bri17_op bri17_op; /* opaque operator handle */
+
+/* Human-readable name of a status code (static storage). */
+const char* bri17_status_string(int status);
+
+/* Last CUDA / validation message recorded by this thread (static storage per
+ * thread; empty string if none). */
+const char* bri17_last_error(void);
+
+/* Library version string, e.g. "0.1.0" (the reference is v0.1,
+ * metadata/version.txt:1). */
+const char* bri17_version(void);
+
+/*
+ * Create an operator for the grid shape[0] x ... x shape[dim-1] of box size
+ * L[0..dim-1] and the isotropic Hooke material (mu, nu).
+ * Replaces: bri17::CartesianGrid<T,DIM>(shape, L) +
+ * bri17::Hooke<T,DIM>(mu, nu, grid)   (include/bri17/bri17.hpp:54-58, :193-194)
+ * plus the FFTW plan set-up of StiffnessMatrixFactory
+ * (tests/test_bri17.cpp:110-128).
+ * dim is 2 or 3; every shape[i] >= 1 and <= 1024 with prime factors <= 61;
+ * L[i] > 0; mu > 0; -1 < nu < 0.5.  Allocates the device work space on the
+ * current CUDA device.
+ */
+int bri17_op_create(int dim, const int* shape, const double* L, double mu,
+                    double nu, int precision, bri17_op** op);
+
+/* Release a handle and its device memory (NULL is accepted). */
+int bri17_op_destroy(bri17_op* op);
+
+/* Grid size |N| (number of nodes = cells) and device work-space bytes. */
+int bri17_op_info(const bri17_op* op, int64_t* size, int64_t* workspace_bytes);
+
+/*
+ * Per-pass timing (diagnostics; no reference counterpart).  While enabled,
+ * each operator application on this handle records CUDA events around each
+ * of its kernel launches, on the launch stream.  bri17_op_pass_times
+ * synchronises those events and returns, per pass id, the summed device time
+ * in ms and the number of launches since the previous call, then resets.
+ * Pass ids: 0 rows_r2c, 1 axis1 forward, 2 axis0 fused, 3 axis1 inverse,
+ * 4 rows_c2r (2D handles have no axis-1 passes).
+ */
+int bri17_op_set_pass_timing(bri17_op* op, int enable);
+int bri17_op_pass_times(bri17_op* op, double* ms, int64_t* launches,
+                        int max_passes, int* npasses);
+const char* bri17_pass_name(int pass);
+
+/* Change the material of an existing handle (no reallocation). */
+int bri17_op_set_material(bri17_op* op, double mu, double nu);
+
+/*
+ * Batched Hooke::modal_stiffness (include/bri17/bri17.hpp:247-292; exported
+ * to Python as Hooke*f64.modal_stiffness_matrix, python/pybri17.cpp:82-87).
+ * k_dev: n x dim int32 multi-indices; K_dev: n x dim x dim complex (row-major
+ * per mode).  For 0 <= k[i] < shape[i] the values equal the reference's bit
+ * for bit; other k are reduced modulo shape[i] first.
+ */
+int bri17_modal_stiffness_batch(const bri17_op* op, const int* k_dev,
+                                int64_t n, void* K_dev, void* stream);
+
+/*
+ * Batched Hooke::modal_strain_displacement (include/bri17/bri17.hpp:212-236,
+ * python/pybri17.cpp:76-81).  B_dev: n x dim complex.
+ */
+int bri17_modal_strain_displacement_batch(const bri17_op* op, const int* k_dev,
+                                          int64_t n, void* B_dev,
+                                          void* stream);
+
+/*
+ * Batched Hooke::modal_eigenstress_to_opposite_strain
+ * (include/bri17/bri17.hpp:308-355, python/pybri17.cpp:88-95).
+ * tau_dev: n x sym complex Mandel components (sym = 3 in 2D, 6 in 3D, order
+ * xx,yy[,zz],[yz,zx,]xy with sqrt(2) on the shears); eta_dev: n x sym complex.
+ * k = 0 gives 0, as in the reference.
+ */
+int bri17_modal_eigenstress_to_opposite_strain_batch(const bri17_op* op,
+                                                     const int* k_dev,
+                                                     int64_t n,
+                                                     const void* tau_dev,
+                                                     void* eta_dev,
+                                                     void* stream);
+
+/*
+ * f = K u: the periodic stiffness operator, computed as
+ * f = (|h|/|N|) IDFT(K(k) DFT(u)(k)), i.e. StiffnessMatrixFactory::compute_Ku
+ * (tests/test_bri17.cpp:56-107), on real fields.  u_dev and f_dev are
+ * dim x size real arrays of the handle's scalar type; they may alias.
+ */
+int bri17_apply_stiffness(bri17_op* op, const void* u_dev, void* f_dev,
+                          void* stream);
+
+/*
+ * Same operator with host buffers: copies u to the device, applies, copies f
+ * back, and synchronises `stream`.  Pinned host memory gives full copy speed.
+ */
+int bri17_apply_stiffness_host(bri17_op* op, const void* u_host, void* f_host,
+                               void* stream);
+
+/*
+ * eps = B u: cell-averaged strains (Mandel, sym components) of nodal
+ * displacements, StrainDisplacementMatrixFactory::compute_Bu
+ * (tests/test_bri17.cpp:194-245).  eps_dev: sym x size real.
+ */
+int bri17_apply_strain(bri17_op* op, const void* u_dev, void* eps_dev,
+                       void* stream);
+
+/*
+ * Nodal forces of a cell-wise eigenstress: b = -|h| B^T tau, computed in
+ * Fourier space as b_hat = -|h| tau_hat . conj(B(k)) (the right-hand side of
+ * include/bri17/bri17.hpp:340).  tau_dev: sym x size real (Mandel);
+ * b_dev: dim x size real.  b has zero mean.
+ */
+int bri17_eigenstress_rhs(bri17_op* op, const void* tau_dev, void* b_dev,
+                          void* stream);
+
+/* Conjugate-gradient modes. */
+typedef enum bri17_cg_mode {
+  BRI17_CG_PLAIN = 0, /* CG in the handle's precision */
+  BRI17_CG_MIXED = 1  /* FP32 inner CG + FP64 residual/refinement outer loop */
+} bri17_cg_mode;
+
+typedef struct bri17_cg_info {
+  int iterations;        /* total operator applications inside CG */
+  int outer_iterations;  /* refinement steps (mixed mode), else 1 */
+  double rel_residual;   /* final ||b - K x|| / ||b|| (FP64, recomputed) */
+  int status;            /* bri17_status of the solve */
+} bri17_cg_info;
+
+/*
+ * Solve K x = b by conjugate gradients, to ||b - K x|| <= tol ||b||, with x
+ * projected to zero mean per component (the null space of K is the rigid
+ * translations, sphinx/theory.rst eq. (17) note).  b_dev and x_dev are FP64
+ * (dim x size).  On entry x_dev is the initial guess (zero it for a cold
+ * start).  BRI17_CG_MIXED needs an FP64 handle; it builds an FP32 twin
+ * internally on first use.  Synchronises `stream` (the stopping test reads
+ * the residual).
+ */
+int bri17_cg_solve(bri17_op* op, const double* b_dev, double* x_dev,
+                   double tol, int max_iterations, int mode,
+                   bri17_cg_info* info, void* stream);
+
+/*
+ * Serving: a continuous-batching solve server on the current device.
+ * Requests (3D eigenstress problems of any supported grid and material) are
+ * admitted while their device footprint fits in `memory_budget_bytes`,
+ * solved concurrently in mixed precision, and retired when converged.
+ */
+typedef struct bri17_server bri17_server;
+
+typedef struct bri17_request_result {
+  int64_t id;
+  int status;             /* bri17_status */
+  int iterations;
+  int outer_iterations;
+  double rel_residual;
+  double submit_time_s;   /* server clock at submit / admit / finish */
+  double admit_time_s;
+  double finish_time_s;
+} bri17_request_result;
+
+int bri17_server_create(int64_t memory_budget_bytes, int max_active,
+                        bri17_server** srv);
+int bri17_server_destroy(bri17_server* srv);
+
+/*
+ * Submit one eigenstress solve.  tau_host: 6 x size FP64 Mandel eigenstress
+ * (copied at submit); the server owns the request until bri17_server_poll
+ * returns it.  x_host: dim x size FP64, written with the solution when the
+ * request finishes (must stay valid until then).  Returns the request id in
+ * *id.
+ */
+int bri17_server_submit(bri17_server* srv, const int* shape, const double* L,
+                        double mu, double nu, const double* tau_host,
+                        double* x_host, double tol, int max_iterations,
+                        int64_t* id);
+
+/* Advance the server: admit, run one scheduling quantum, retire.  Returns
+ * the number of active requests in *active. */
+int bri17_server_step(bri17_server* srv, int* active);
+
+/* Pop up to `cap` finished results; *count receives how many. */
+int bri17_server_poll(bri17_server* srv, bri17_request_result* out, int cap,
+                      int* count);
+
+/* Cancel a queued or running request (its result reports CANCELLED). */
+int bri17_server_cancel(bri17_server* srv, int64_t id);
+
+/* Server clock (seconds since creation). */
+double bri17_server_clock(const bri17_server* srv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BRI17_GB300_H_ */

@@ -1,0 +1,183 @@
+"""GPU parity of the periodic stiffness operator (CUDA path through the C
+ABI) against the oracle and the reference's golden element matrices."""
+import numpy as np
+import pytest
+
+from gpu_helpers import mean_free_normal, pair, rel_l2, to_dev
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+# Floating-point tolerances (relative l2, FP64 / FP32 operator vs oracle).
+TOL_F64 = 1e-12
+TOL_F32 = 2e-5
+
+
+def _dense_from_gpu(fn, ncols, nrows, dtype):
+    import torch
+    M = np.empty((nrows, ncols))
+    e = torch.zeros(ncols, dtype=dtype, device="cuda")
+    for j in range(ncols):
+        e.zero_()
+        e[j] = 1.0
+        M[:, j] = fn(e).reshape(-1).double().cpu().numpy()
+    return M
+
+
+@pytest.mark.parametrize("case_index", [0, 1, 2, 3])
+def test_golden_element_matrices(golden_elements, case_index):
+    """tests/test_bri17.cpp:335-605 on the GPU: K (B) extracted by unit
+    vectors equals the assembly of the Maxima element matrix,
+    |a - e| <= 1e-15 |e| + 1e-14."""
+    import torch
+    g = golden_elements
+    case = g["cases"][case_index]
+    h, ho = pair(case["shape"], case["L"], g["mu"], g["nu"])
+    grid = ho.grid
+    E = np.array(case["values"]).reshape(case["rows"], case["cols"])
+    n = grid.dim * grid.size
+    if case["kind"] == "K":
+        expected = O.assemble_stiffness(grid, E)
+        actual = _dense_from_gpu(
+            lambda e: h.apply_stiffness(e.reshape((grid.dim,) + grid.shape)), n, n,
+            torch.float64)
+    else:
+        sym = 3 if grid.dim == 2 else 6
+        expected = O.assemble_strain_displacement(grid, E)
+        actual = _dense_from_gpu(
+            lambda e: h.apply_strain(e.reshape((grid.dim,) + grid.shape)), n,
+            sym * grid.size, torch.float64)
+    err = np.abs(actual - expected)
+    tol = g["rtol"] * np.abs(expected) + g["atol"]
+    assert np.all(err <= tol), f"max excess {(err - tol).max()}"
+
+
+SHAPES = [
+    ((64, 64), (1.0, 1.0), 1.0, 0.3),          # 2D Q4 64x64 case
+    ((3, 4), (3.3, 4.8), 5.6, 0.3),
+    ((5, 7), (1.0, 2.0), 2.0, 0.1),
+    ((6, 10), (0.5, 1.5), 1.0, 0.45),
+    ((48, 96), (1.0, 2.0), 0.7, 0.2),
+    ((1, 8), (1.0, 1.0), 1.0, 0.3),
+    ((3, 4, 5), (3.3, 4.8, 6.5), 5.6, 0.3),
+    ((8, 8, 8), (1.0, 1.0, 1.0), 1.0, 0.25),
+    ((6, 10, 8), (1.0, 2.5, 0.75), 1.7, 0.45),
+    ((12, 9, 7), (1.0, 1.0, 0.125), 0.5, 0.1),
+    ((32, 48, 20), (1.0, 1.5, 0.6), 1.0, 0.3),
+    ((7, 11, 13), (1.0, 1.0, 1.0), 1.0, 0.3),   # generic odd radices
+    ((14, 21, 22), (2.0, 1.0, 1.0), 1.2, 0.35),
+    ((96, 32, 64), (3.0, 1.0, 2.0), 1.0, 0.3),
+    ((16, 4, 1), (1.0, 1.0, 1.0), 1.0, 0.3),    # degenerate last axis
+    ((1, 6, 10), (1.0, 1.0, 1.0), 1.0, 0.3),    # degenerate first axis
+]
+
+
+@pytest.mark.parametrize("shape,L,mu,nu", SHAPES)
+def test_operator_matches_oracle_f64(shape, L, mu, nu):
+    h, ho = pair(shape, L, mu, nu)
+    rng = np.random.default_rng(0)
+    u = mean_free_normal(rng, len(shape), shape)
+    f = h.apply_stiffness(to_dev(u)).cpu().numpy()
+    f_ref = O.apply_stiffness(ho, u)
+    assert rel_l2(f, f_ref) <= TOL_F64
+
+
+@pytest.mark.parametrize("shape,L,mu,nu", SHAPES[::3])
+def test_operator_matches_oracle_f32(shape, L, mu, nu):
+    import torch
+    h, ho = pair(shape, L, mu, nu, precision="f32")
+    rng = np.random.default_rng(1)
+    u = mean_free_normal(rng, len(shape), shape).astype(np.float32)
+    f = h.apply_stiffness(to_dev(u)).cpu().numpy().astype(np.float64)
+    f_ref = O.apply_stiffness(ho, u.astype(np.float64))
+    assert rel_l2(f, f_ref) <= TOL_F32
+
+
+def test_operator_128_cubed_matches_oracle():
+    """3D 128^3, h = 1/128, mu = 1, nu = 0.25, u ~ N(0,1) seeded, mean-free."""
+    shape = (128, 128, 128)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.25)
+    rng = np.random.default_rng(1)
+    u = mean_free_normal(rng, 3, shape)
+    f = h.apply_stiffness(to_dev(u)).cpu().numpy()
+    assert rel_l2(f, O.apply_stiffness(ho, u)) <= TOL_F64
+
+
+def test_operator_properties():
+    """Symmetry, rigid translations in the null space, linearity, aliasing,
+    bitwise determinism."""
+    import torch
+    shape = (24, 20, 18)
+    h, _ = pair(shape, (1.0, 0.8, 1.2), 1.3, 0.3)
+    rng = np.random.default_rng(2)
+    u = to_dev(rng.standard_normal((3,) + shape))
+    v = to_dev(rng.standard_normal((3,) + shape))
+    Ku, Kv = h.apply_stiffness(u), h.apply_stiffness(v)
+    a, b = float((v * Ku).sum()), float((u * Kv).sum())
+    assert abs(a - b) <= 1e-12 * abs(a)
+    c = torch.ones((3,) + shape, dtype=torch.float64, device="cuda")
+    c[1] *= -2.5
+    assert float(h.apply_stiffness(c).abs().max()) <= 1e-12 * float(Ku.abs().max())
+    w = h.apply_stiffness(2.0 * u - 3.0 * v)
+    assert float((w - (2.0 * Ku - 3.0 * Kv)).norm() / w.norm()) <= 1e-13
+    again = h.apply_stiffness(u)
+    assert torch.equal(again, Ku)
+    alias = u.clone()
+    h.apply_stiffness(alias, out=alias)
+    assert torch.equal(alias, Ku)
+
+
+def test_host_buffer_entry_point():
+    shape = (16, 12, 10)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3)
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((3,) + shape)
+    f = h.apply_stiffness_host(u)
+    assert rel_l2(f, O.apply_stiffness(ho, u)) <= TOL_F64
+    assert np.array_equal(f, h.apply_stiffness(to_dev(u)).cpu().numpy())
+
+
+def test_modal_batch_matches_reference_fixture(golden_modal):
+    """Batched Hooke::modal_stiffness equals the reference header's output
+    bit for bit for in-range k; B and out-of-range K to 1e-15."""
+    for c in golden_modal:
+        h, _ = pair(c["shape"], c["L"], c["mu"], c["nu"])
+        k = c["k"]
+        dim = len(c["shape"])
+        K = h.modal_stiffness_batch(k).cpu().numpy().reshape(len(k), -1)
+        B = h.modal_strain_displacement_batch(k).cpu().numpy()
+        inr = np.all((k >= 0) & (k < np.array(c["shape"])), axis=1)
+        assert np.array_equal(K[inr].view(np.float64), c["K"][inr].view(np.float64))
+        scale = np.abs(c["K"]).max()
+        assert np.abs(K - c["K"]).max() <= 1e-15 * scale * 4
+        bscale = np.abs(c["B"]).max()
+        assert np.abs(B - c["B"]).max() <= 1e-15 * bscale * 4
+
+
+def test_modal_eigenstress_batch_matches_oracle():
+    shape, L = (6, 10, 8), (1.0, 2.5, 0.75)
+    h, ho = pair(shape, L, 1.7, 0.45)
+    rng = np.random.default_rng(6)
+    grids = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+    k = np.stack([x.ravel() for x in grids], 1).astype(np.intc)
+    tau = rng.standard_normal((len(k), 6)) + 1j * rng.standard_normal((len(k), 6))
+    eta = h.modal_eigenstress_to_opposite_strain_batch(k, tau).cpu().numpy()
+    ref = np.array([ho.modal_eigenstress_to_opposite_strain(kk, t) for kk, t in zip(k, tau)])
+    assert np.abs(eta - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert np.all(eta[0] == 0)
+
+
+def test_pybri17_per_mode_methods(golden_modal):
+    from bri17_gb300 import pybri17
+    c = golden_modal[1]
+    grid = pybri17.CartesianGrid3f64(tuple(c["shape"]), tuple(c["L"]))
+    h = pybri17.Hooke3f64(c["mu"], c["nu"], grid)
+    for i in (0, 7, 33, 59):
+        K = np.zeros(9, dtype=np.complex128)
+        B = np.zeros(3, dtype=np.complex128)
+        h.modal_stiffness_matrix(c["k"][i], K)
+        h.modal_strain_displacement(c["k"][i], B)
+        assert np.array_equal(K, c["K"][i])
+        assert np.abs(B - c["B"][i]).max() <= 4e-15 * np.abs(c["B"]).max()
+    with pytest.raises(ValueError):
+        h.modal_stiffness_matrix(c["k"][0], np.zeros((3, 3), np.complex128))

@@ -1,0 +1,82 @@
+"""GPU parity of the eigenstress right-hand side, the strain map and the CG
+solvers against the oracle (the exact per-mode solve of
+include/bri17/bri17.hpp:308-355)."""
+import numpy as np
+import pytest
+
+from gpu_helpers import mean_free_normal, pair, rel_l2, to_dev
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("shape,L", [((12, 10), (1.0, 1.2)), ((3, 4, 5), (3.3, 4.8, 6.5)),
+                                     ((16, 12, 10), (1.0, 0.8, 1.1)), ((9, 14, 7), (1., 1., 1.))])
+def test_eigenstress_rhs_matches_oracle(shape, L):
+    h, ho = pair(shape, L, 1.0, 0.3)
+    sym = 3 if len(shape) == 2 else 6
+    tau = np.random.default_rng(7).standard_normal((sym,) + shape)
+    b = h.eigenstress_rhs(to_dev(tau)).cpu().numpy()
+    assert rel_l2(b, O.eigenstress_rhs(ho, tau)) <= 1e-12
+    assert np.abs(b.reshape(len(shape), -1).mean(axis=1)).max() <= 1e-14 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("shape,L", [((12, 10), (1.0, 1.2)), ((16, 12, 10), (1.0, 0.8, 1.1)),
+                                     ((5, 6, 7), (1.0, 1.0, 1.0))])
+def test_strain_matches_oracle(shape, L):
+    h, ho = pair(shape, L, 1.0, 0.3)
+    u = np.random.default_rng(8).standard_normal((len(shape),) + shape)
+    eps = h.apply_strain(to_dev(u)).cpu().numpy()
+    assert rel_l2(eps, O.apply_strain(ho, u)) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+@pytest.mark.parametrize("shape,nu", [((32, 32, 32), 0.3), ((24, 20, 16), 0.45), ((48, 40), 0.3)])
+def test_cg_matches_modal_direct_solve(mode, shape, nu):
+    """CG to 1e-10 relative residual vs the exact FP64 per-mode solve;
+    error <= kappa * residual bounds the difference."""
+    L = (1.0,) * len(shape)
+    h, ho = pair(shape, L, 1.0, nu)
+    sym = 3 if len(shape) == 2 else 6
+    tau = np.random.default_rng(2).standard_normal((sym,) + shape)
+    b = h.eigenstress_rhs(to_dev(tau))
+    x, info = h.cg_solve(b, tol=1e-10, mode=mode)
+    assert info["status"] == 0, info
+    assert info["rel_residual"] <= 1e-10
+    x_ref = O.eigenstress_solve(ho, tau)
+    assert rel_l2(x.cpu().numpy(), x_ref) <= 1e-6
+    # The returned residual is the FP64 one.
+    r = b - h.apply_stiffness(x)
+    assert float(r.norm() / b.norm()) <= 1.01e-10
+
+
+def test_cg_edge_cases():
+    import torch
+    h, _ = pair((8, 8, 8), (1.0, 1.0, 1.0), 1.0, 0.3)
+    zero = torch.zeros((3, 8, 8, 8), dtype=torch.float64, device="cuda")
+    x, info = h.cg_solve(zero, tol=1e-8)
+    assert info["status"] == 0 and float(x.abs().max()) == 0.0
+    tau = np.random.default_rng(3).standard_normal((6, 8, 8, 8))
+    b = h.eigenstress_rhs(to_dev(tau))
+    x, info = h.cg_solve(b, tol=1e-14, max_iterations=3, raise_on_failure=False)
+    assert info["status"] == 5  # not converged
+    bad = b.clone()
+    bad[0, 0, 0, 0] = float("nan")
+    x, info = h.cg_solve(bad, tol=1e-8, raise_on_failure=False)
+    assert info["status"] == 6  # breakdown
+    # The handle stays usable after a breakdown.
+    x, info = h.cg_solve(b, tol=1e-8)
+    assert info["status"] == 0
+
+
+def test_cg_warm_start_and_material_change():
+    h, ho = pair((16, 16, 16), (1.0, 1.0, 1.0), 1.0, 0.3)
+    tau = np.random.default_rng(4).standard_normal((6, 16, 16, 16))
+    b = h.eigenstress_rhs(to_dev(tau))
+    x, info = h.cg_solve(b, tol=1e-6)
+    x2, info2 = h.cg_solve(b, x0=x, tol=1e-10)
+    assert info2["iterations"] < 200 and info2["rel_residual"] <= 1e-10
+    h.set_material(2.0, 0.2)
+    ho2 = O.Hooke(2.0, 0.2, ho.grid)
+    x3, info3 = h.cg_solve(b, tol=1e-10, mode="mixed")
+    assert rel_l2(x3.cpu().numpy(), O.eigenstress_solve(ho2, tau)) <= 1e-6
