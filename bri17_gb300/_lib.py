@@ -70,6 +70,8 @@ _SIGS = {
         [vp, vp, ctypes.c_int64, vp, vp, vp], ctypes.c_int),
     "bri17_apply_stiffness": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_apply_stiffness_host": ([vp, vp, vp, vp], ctypes.c_int),
+    "bri17_apply_stiffness_noalloc": ([ctypes.c_int, c_int_p, c_double_p, ctypes.c_double,
+                                       ctypes.c_double, vp, vp, vp], ctypes.c_int),
     "bri17_apply_strain": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_eigenstress_rhs": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_cg_solve": ([vp, vp, vp, ctypes.c_double, ctypes.c_int, ctypes.c_int,

@@ -156,6 +156,30 @@ int bri17_apply_stiffness(bri17_op* op, const void* u_dev, void* f_dev,
                           void* stream);
 
 /*
+ * f = K u without any device allocation (FP64).  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory -- a
+ * plugin whose host application owns every device allocation and forbids
+ * cudaMalloc, code held to a device-memory budget fixed in advance, or a
+ * caller that must not let cudaMalloc/cudaFree synchronise the device.
+ * The caller passes the grid, the material, u_dev and f_dev (dim x size FP64
+ * device arrays, SoA, as bri17_apply_stiffness); results equal
+ * bri17_apply_stiffness's.
+ * Scratch (per-axis tables + the FP64 half spectrum) lives in one fixed
+ * 64 MiB device array that every GPU loading this library holds until the
+ * process exits; grids needing more (tables + dim * n0 * n1 * (n2/2+1) * 16
+ * bytes, e.g. anything above 128^3) return BRI17_ERR_UNSUPPORTED_SIZE.
+ * The first call on a device looks up that array's device address on that
+ * device (set-up), so make the first call before any stream capture.  Every
+ * call shares the one array and rewrites all of it that it reads (nothing
+ * needs to start at zero); calls whose GPU work overlaps -- on different
+ * streams, or from different threads -- race on it and must be serialised by
+ * the caller.
+ */
+int bri17_apply_stiffness_noalloc(int dim, const int* shape, const double* L,
+                                  double mu, double nu, const double* u_dev,
+                                  double* f_dev, void* stream);
+
+/*
  * Same operator with host buffers: copies u to the device, applies, copies f
  * back, and synchronises `stream`.  Pinned host memory gives full copy speed.
  */
