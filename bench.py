@@ -372,14 +372,249 @@ def run_operator(args, precision="f64"):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# CG workloads (256^3 eigenstress solve; anisotropic 512x512x128).
+
+WORKLOAD_CG = dict(shape=(256, 256, 256), L=(1.0, 1.0, 1.0), mu=1.0, nu=0.3, seed=2)
+WORKLOAD_ANISO = dict(shape=(512, 512, 128), L=(1.0, 1.0, 0.125), mu=1.0, nu=0.35, seed=4)
+
+
+def tau_normal(shape, seed):
+    return np.random.default_rng(seed).standard_normal((6,) + tuple(shape))
+
+
+def tau_inclusions(shape, L, seed):
+    """Two z-through columns (centres (0.25, 0.25, Lz/2) and (0.75, 0.75,
+    Lz/2), periodic minimum-image distance, radius 0.2): all six Mandel
+    components 1 inside, 0 outside, plus N(0, 0.01^2) noise."""
+    rng = np.random.default_rng(seed)
+    ax = [(np.arange(n) + 0.5) * (Li / n) for n, Li in zip(shape, L)]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    inside = np.zeros(shape, dtype=bool)
+    for c in ((0.25, 0.25, L[2] / 2), (0.75, 0.75, L[2] / 2)):
+        d2 = 0.0
+        for coord, cc, Li in zip((X, Y, Z), c, L):
+            dd = np.abs(coord - cc)
+            dd = np.minimum(dd, Li - dd)
+            d2 = d2 + dd * dd
+        inside |= d2 <= 0.2 ** 2
+    tau = rng.normal(0.0, 0.01, size=(6,) + tuple(shape))
+    tau += inside[None].astype(np.float64)
+    return tau
+
+
+def oracle_solution(w, tau, threads):
+    from oracle import oracle as O
+    O.set_num_threads(threads)
+    h = O.Hooke(w["mu"], w["nu"], O.Grid(w["shape"], w["L"]))
+    return O.eigenstress_solve(h, tau)
+
+
+def run_cg(args, w, tau_fn, label):
+    import torch
+
+    from bri17_gb300 import CartesianGrid, Hooke
+    torch.cuda.set_device(0)
+    shape = w["shape"]
+    dof = 3 * int(np.prod(shape))
+    tau_np = tau_fn()
+    hooke = Hooke(w["mu"], w["nu"], CartesianGrid(shape, w["L"]))
+    tau = torch.from_numpy(tau_np).cuda()
+    b = hooke.eigenstress_rhs(tau)
+    del tau
+    out = {}
+    sols = {}
+    sampler = ClockSampler(0)
+    sampler.start()
+    for mode in ("mixed", "plain"):
+        # warm-up: a short solve captures the graphs and builds the FP32 twin
+        hooke.cg_solve(b, tol=1e-2, mode=mode, raise_on_failure=False)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            x, info = hooke.cg_solve(b, tol=1e-8, mode=mode, max_iterations=200000)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        sols[mode] = x
+        out[mode] = {"solves_per_s": 1.0 / statistics.median(times),
+                     "seconds_per_solve": statistics.median(times),
+                     "iterations": info["iterations"],
+                     "outer_iterations": info["outer_iterations"],
+                     "rel_residual": info["rel_residual"]}
+    clocks = sampler.stop()
+    err = {}
+    if not args.no_oracle:
+        t0 = time.perf_counter()
+        x_ref = oracle_solution(w, tau_np, os.cpu_count() or 1)
+        nref = np.linalg.norm(x_ref)
+        for mode in sols:
+            err[mode] = float(np.linalg.norm(sols[mode].cpu().numpy() - x_ref) / nref)
+        err["oracle_seconds"] = time.perf_counter() - t0
+    line = {
+        "metric": METRIC, "value": out["mixed"]["solves_per_s"], "unit": "solves/s",
+        "n_gpus": 1, "steps": max(1, args.steps), "warmup": 1, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+        "data": "synthetic",
+        "config": {"workload": label, "grid": list(shape), "dof": dof, "tol": 1e-8,
+                   "mu": w["mu"], "nu": w["nu"], "seed": w["seed"]},
+        "mixed": out["mixed"], "fp64": out["plain"],
+        "mixed_over_fp64_speedup": out["mixed"]["solves_per_s"] / out["plain"]["solves_per_s"],
+        "error_vs_fp64_oracle": err, "clocks": clocks,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# Serving workload: 512 requests, Poisson arrivals (mean 5 ms), cubic sides
+# from {32, 48, 64, 96, 128}, mu ~ U[0.5, 2], nu ~ U[0.1, 0.45],
+# tau ~ N(0, 1), tol 1e-8, seed 3.
+
+def serve_requests(n, seed):
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(0.005, size=n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sides = rng.choice([32, 48, 64, 96, 128], size=n)
+    mus = rng.uniform(0.5, 2.0, size=n)
+    nus = rng.uniform(0.1, 0.45, size=n)
+    return [dict(i=i, t=float(arrivals[i]), side=int(sides[i]), mu=float(mus[i]),
+                 nu=float(nus[i]), seed=seed * 100003 + i) for i in range(n)]
+
+
+def make_tau(req):
+    s = req["side"]
+    return np.random.default_rng(req["seed"]).standard_normal((6, s, s, s))
+
+
+def run_serve(args):
+    import queue
+    import threading
+
+    import torch
+
+    from bri17_gb300 import CartesianGrid, Hooke
+    from bri17_gb300.server import Server
+    torch.cuda.set_device(0)
+    nreq = args.requests
+    reqs = serve_requests(nreq, 3)
+    # tau is generated ahead of arrival on a producer thread (numpy releases
+    # the GIL while filling); at most ~4 GB in flight.
+    q = queue.Queue(maxsize=48)
+
+    def producer():
+        for r in reqs:
+            q.put((r, make_tau(r)))
+    threading.Thread(target=producer, daemon=True).start()
+    srv = Server(memory_budget_bytes=args.memory_gb << 30, slots_per_bucket=args.slots)
+    # Warm the buckets (graph capture, first-touch) with one tiny solve per size.
+    for s in (32, 48, 64, 96, 128):
+        srv.submit((s, s, s), (1, 1, 1), 1.0, 0.3, np.zeros((6, s, s, s)), tol=1e-8)
+    srv.run_until_idle()
+    sampler = ClockSampler(0)
+    sampler.start()
+    t_start = srv.clock()
+    submitted, done, ready = 0, {}, None
+    meta = {}
+    while len(done) < nreq:
+        now = srv.clock() - t_start
+        while submitted < nreq:
+            if ready is None:
+                try:
+                    ready = q.get(timeout=0.0 if srv.pending else 0.05)
+                except Exception:
+                    break
+            r, tau = ready
+            if r["t"] > now:
+                break
+            s = r["side"]
+            rid = srv.submit((s, s, s), (1, 1, 1), r["mu"], r["nu"], tau, tol=1e-8)
+            meta[rid] = r
+            submitted += 1
+            ready = None
+        if srv.pending:
+            srv.step()
+            for res in srv.poll():
+                if res["id"] in meta:
+                    done[res["id"]] = res
+                srv.result(res["id"])
+        else:
+            time.sleep(0.0005)
+    makespan = max(d["finish_time_s"] for d in done.values()) - t_start
+    clocks = sampler.stop()
+    lat = np.array([done[i]["finish_time_s"] - t_start - meta[i]["t"] for i in done])
+    ok = sum(1 for d in done.values() if d["status"] == 0)
+    srv.close()
+
+    # One-at-a-time FP64 baseline on a subsample (2 per size), then a FIFO
+    # single-server queue over the same arrivals with per-size service times.
+    service = {}
+    hookes = {}
+    sub = []
+    for s in (32, 48, 64, 96, 128):
+        sub += [r for r in reqs if r["side"] == s][: args.baseline_per_size]
+    for r in sub:
+        s = r["side"]
+        if s not in hookes:
+            hookes[s] = Hooke(1.0, 0.3, CartesianGrid((s, s, s), (1, 1, 1)))
+            hookes[s].cg_solve(hookes[s].eigenstress_rhs(
+                torch.zeros((6, s, s, s), dtype=torch.float64, device="cuda")), tol=1e-8)
+        tau = make_tau(r)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = hookes[s]
+        h.set_material(r["mu"], r["nu"])
+        b = h.eigenstress_rhs(torch.from_numpy(tau).cuda())
+        x, info = h.cg_solve(b, tol=1e-8, mode="plain")
+        x.cpu()
+        service.setdefault(s, []).append(time.perf_counter() - t0)
+    mean_service = {s: float(np.mean(v)) for s, v in service.items()}
+    tq, lat_b = 0.0, []
+    for r in reqs:
+        start = max(tq, r["t"])
+        tq = start + mean_service[r["side"]]
+        lat_b.append(tq - r["t"])
+    base_makespan = tq
+    line = {
+        "metric": METRIC, "value": nreq / makespan, "unit": "solves/s", "n_gpus": 1,
+        "steps": nreq, "warmup": 5, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inner / f64 outer", "data": "synthetic",
+        "config": {"workload": "serving stream: 512 eigenstress CG solves, Poisson arrivals "
+                               "mean 5 ms, cubic sides {32,48,64,96,128}, mu~U[0.5,2], "
+                               "nu~U[0.1,0.45], tau~N(0,1), tol 1e-8, seed 3",
+                   "slots_per_bucket": args.slots, "memory_budget_gb": args.memory_gb},
+        "batched_mixed": {"solves_per_s": nreq / makespan, "makespan_s": makespan,
+                          "p50_latency_s": float(np.percentile(lat, 50)),
+                          "p99_latency_s": float(np.percentile(lat, 99)),
+                          "succeeded": ok},
+        "one_at_a_time_fp64": {"solves_per_s": nreq / base_makespan,
+                               "makespan_s": base_makespan,
+                               "p50_latency_s": float(np.percentile(lat_b, 50)),
+                               "p99_latency_s": float(np.percentile(lat_b, 99)),
+                               "service_s_per_size": mean_service,
+                               "method": f"{args.baseline_per_size} measured solves per size, "
+                                         "FIFO queue over the same arrivals"},
+        "note": "offered load (200/s) exceeds capacity: latency includes queueing",
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="operator", choices=["operator", "operator_f32"])
+    ap.add_argument("--workload", default="operator",
+                    choices=["operator", "operator_f32", "cg", "aniso", "serve"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true")
+    ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--memory-gb", type=int, default=48)
+    ap.add_argument("--baseline-per-size", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -387,6 +622,16 @@ def main():
         return run_reference(args)
     if args.workload == "operator_f32":
         return run_operator(args, precision="f32")
+    if args.workload == "cg":
+        return run_cg(args, WORKLOAD_CG, lambda: tau_normal(WORKLOAD_CG["shape"], 2),
+                      "3D 256^3 eigenstress CG to 1e-8, mu=1 nu=0.3, tau~N(0,1) seed 2")
+    if args.workload == "aniso":
+        w = WORKLOAD_ANISO
+        return run_cg(args, w, lambda: tau_inclusions(w["shape"], w["L"], 4),
+                      "3D 512x512x128, h=(1/512,1/512,1/1024), mu=1 nu=0.35, two-column "
+                      "inclusion eigenstress + N(0,0.01) noise, seed 4")
+    if args.workload == "serve":
+        return run_serve(args)
     return run_operator(args)
 
 

@@ -48,10 +48,12 @@ int apply_stiffness_async(bri17_op* op, const void* u, void* f,
 // Batched forms used by the server: `batch` fields of one geometry,
 // contiguous (entry z at z * dim * size), with per-entry material
 // (s, mu) pairs in `mat` (device, precision of the handle, already scaled by
-// |h|/|N|).  spec must hold batch * dim * cspec complex values.
+// |h|/|N|).  spec must hold batch * dim * cspec complex values.  `flags`
+// (optional, device) skips entry z when flags[z * flag_stride] == 0.
 int apply_stiffness_batched_async(bri17_op* op, int batch, const void* u,
                                   void* f, void* spec, const void* mat,
-                                  cudaStream_t stream);
+                                  cudaStream_t stream, const int* flags = nullptr,
+                                  int flag_stride = 0);
 int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
                                   void* b, void* spec, cudaStream_t stream);
 

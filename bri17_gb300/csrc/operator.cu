@@ -195,52 +195,64 @@ static void set_smem_attrs() {
   });
 }
 
+// Rows per CTA for the last-axis passes: about kTileElems complex values,
+// and, when a batch mask is in use, a divisor of the rows of one entry so
+// that no CTA straddles two entries.
+static int rows_per_cta(int m, int64_t nrows, int64_t rows_per_entry, bool masked) {
+  int64_t r = std::max<int64_t>(1, std::min<int64_t>(nrows, kTileElems / m));
+  if (masked) {
+    while (r > 1 && rows_per_entry % r != 0) r--;
+  }
+  return (int)r;
+}
+
 template <typename T>
 static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
-                           int64_t nrows, const Tables<T>& tab,
+                           int64_t nrows, const Tables<T>& tab, BatchMask mask,
                            cudaStream_t st) {
   const int n = g.n[g.dim - 1];
   const int m = (n % 2 == 0) ? n / 2 : n;
   const int pitch = m + 1;
-  int rows = (int)std::max<int64_t>(1, std::min<int64_t>(nrows, kTileElems / m));
+  const int rows = rows_per_cta(m, nrows, mask.unit, mask.flags != nullptr);
   size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)rows * pitch * sizeof(cplx<T>);
   const int64_t grid = (nrows + rows - 1) / rows;
   rows_r2c<T><<<(unsigned)grid, kThreads, smem, st>>>(x, X, nrows, n, g.H, g.plan_row,
-                                                      tab.tw[g.dim - 1], rows, pitch);
+                                                      tab.tw[g.dim - 1], rows, pitch, mask);
   return BRI17_OK;
 }
 
 template <typename T>
 static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
-                           int64_t nrows, const Tables<T>& tab,
+                           int64_t nrows, const Tables<T>& tab, BatchMask mask,
                            cudaStream_t st) {
   const int n = g.n[g.dim - 1];
   const int m = (n % 2 == 0) ? n / 2 : n;
   const int pitch = m + 1;
-  int rows = (int)std::max<int64_t>(1, std::min<int64_t>(nrows, kTileElems / m));
+  const int rows = rows_per_cta(m, nrows, mask.unit, mask.flags != nullptr);
   size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)rows * pitch * sizeof(cplx<T>);
   const int64_t grid = (nrows + rows - 1) / rows;
   rows_c2r<T><<<(unsigned)grid, kThreads, smem, st>>>(X, x, nrows, n, g.H, g.plan_row,
-                                                      tab.tw[g.dim - 1], rows, pitch);
+                                                      tab.tw[g.dim - 1], rows, pitch, mask);
   return BRI17_OK;
 }
 
 template <typename T, bool INV>
 static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
-                        const Tables<T>& tab, cudaStream_t st) {
+                        const Tables<T>& tab, BatchMask mask, cudaStream_t st) {
   const int n = g.n[1];
   const int64_t B = g.H;
   const int pitch = n + 1;
   int TB = (int)std::min<int64_t>(B, std::max(4, std::min(32, kTileElems / n)));
   size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)TB * pitch * sizeof(cplx<T>);
   dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);
-  axis_c2c<T, INV><<<grid, kThreads, smem, st>>>(X, n, B, TB, pitch, g.plan[1], tab.tw[1]);
+  axis_c2c<T, INV><<<grid, kThreads, smem, st>>>(X, n, B, TB, pitch, g.plan[1], tab.tw[1],
+                                                mask);
   return BRI17_OK;
 }
 
 template <typename T, int DIM, int MODE>
 static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
-                        int64_t bstride, const FusedParams<T>& fp,
+                        int64_t bstride, const FusedParams<T>& fp, BatchMask mask,
                         cudaStream_t st) {
   constexpr int SYM = DIM == 2 ? 3 : 6;
   constexpr int CIN = MODE == kModeRhs ? SYM : DIM;
@@ -263,7 +275,7 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
   size_t smem = n0 * sizeof(cplx<T>) + (size_t)TB * per_line;
   dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
   axis0_fused<T, DIM, MODE><<<grid, kThreads, smem, st>>>(
-      X, n0, g.P, g.cspec, bstride, TB, pitch, g.plan[0], fp);
+      X, n0, g.P, g.cspec, bstride, TB, pitch, g.plan[0], fp, mask);
   return BRI17_OK;
 }
 
@@ -346,11 +358,15 @@ struct PassScope {
 };
 
 // Generic three- or five-pass pipeline: forward rows (+ axis 1), fused axis
-// 0, inverse axis 1 (+ rows).  `in` has cin components, `out` cout.
+// 0, inverse axis 1 (+ rows).  `in` has cin components per batch entry,
+// `out` cout; entry z of the spectrum starts at spec + z * cmax * cspec.
+// `flags` (optional) masks batch entries: entry z is skipped when
+// flags[z * flag_stride] == 0.
 template <typename T, int MODE>
 static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
                         T* out, int batch, void* spec, const T* mat,
-                        cudaStream_t st) {
+                        cudaStream_t st, const int* flags = nullptr,
+                        int flag_stride = 0) {
   const Geometry& g = op->g;
   const int dim = g.dim;
   const int sym = dim == 2 ? 3 : 6;
@@ -362,17 +378,30 @@ static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
   cplx<T>* S = reinterpret_cast<cplx<T>*>(spec);
   const int64_t bstride = (int64_t)cmax * g.cspec;
   set_smem_attrs<T>();
-  // Forward rows / axis 1, per batch entry (components contiguous).
-  for (int z = 0; z < batch; z++) {
-    const T* src = in + (int64_t)z * cin * g.size;
-    cplx<T>* Sz = S + z * bstride;
+  // Launch over entries [z0, z0 + nz): one launch when their data are
+  // contiguous (c == cmax or a single entry), else one per entry.
+  auto mask_at = [&](int z0, int64_t unit) {
+    BatchMask m;
+    m.flags = flags ? flags + (int64_t)z0 * flag_stride : nullptr;
+    m.stride = flag_stride;
+    m.unit = unit;
+    return m;
+  };
+  const bool fwd_contig = (cin == cmax) || batch == 1;
+  const bool inv_contig = (cout == cmax) || batch == 1;
+  for (int z0 = 0; z0 < batch; z0 += fwd_contig ? batch : 1) {
+    const int nz = fwd_contig ? batch : 1;
+    const T* src = in + (int64_t)z0 * cin * g.size;
+    cplx<T>* Sz = S + z0 * bstride;
     {
       PassScope ps(op, 0, st);
-      launch_rows_r2c<T>(g, src, Sz, cin * rows_per_comp, tab, st);
+      launch_rows_r2c<T>(g, src, Sz, (int64_t)nz * cin * rows_per_comp, tab,
+                         mask_at(z0, (int64_t)cin * rows_per_comp), st);
     }
     if (dim == 3) {
       PassScope ps(op, 1, st);
-      launch_axis1<T, false>(g, Sz, (int64_t)cin * g.n[0], tab, st);
+      launch_axis1<T, false>(g, Sz, (int64_t)nz * cin * g.n[0], tab,
+                             mask_at(z0, (int64_t)cin * g.n[0]), st);
     }
   }
   FusedParams<T> fp = fused_params<T>(op, tab, MODE);
@@ -381,21 +410,24 @@ static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
   {
     PassScope ps(op, 2, st);
     if (dim == 3)
-      rc = launch_fused<T, 3, MODE>(g, S, batch, bstride, fp, st);
+      rc = launch_fused<T, 3, MODE>(g, S, batch, bstride, fp, mask_at(0, 1), st);
     else
-      rc = launch_fused<T, 2, MODE>(g, S, batch, bstride, fp, st);
+      rc = launch_fused<T, 2, MODE>(g, S, batch, bstride, fp, mask_at(0, 1), st);
   }
   if (rc != BRI17_OK) return rc;
-  for (int z = 0; z < batch; z++) {
-    T* dst = out + (int64_t)z * cout * g.size;
-    cplx<T>* Sz = S + z * bstride;
+  for (int z0 = 0; z0 < batch; z0 += inv_contig ? batch : 1) {
+    const int nz = inv_contig ? batch : 1;
+    T* dst = out + (int64_t)z0 * cout * g.size;
+    cplx<T>* Sz = S + z0 * bstride;
     if (dim == 3) {
       PassScope ps(op, 3, st);
-      launch_axis1<T, true>(g, Sz, (int64_t)cout * g.n[0], tab, st);
+      launch_axis1<T, true>(g, Sz, (int64_t)nz * cout * g.n[0], tab,
+                            mask_at(z0, (int64_t)cout * g.n[0]), st);
     }
     {
       PassScope ps(op, 4, st);
-      launch_rows_c2r<T>(g, Sz, dst, cout * rows_per_comp, tab, st);
+      launch_rows_c2r<T>(g, Sz, dst, (int64_t)nz * cout * rows_per_comp, tab,
+                         mask_at(z0, (int64_t)cout * rows_per_comp), st);
     }
   }
   cudaError_t e = cudaGetLastError();
@@ -431,14 +463,17 @@ int apply_stiffness_async(bri17_op* op, const void* u, void* f,
 
 int apply_stiffness_batched_async(bri17_op* op, int batch, const void* u,
                                   void* f, void* spec, const void* mat,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, const int* flags,
+                                  int flag_stride) {
   if (op->precision == BRI17_F64)
     return run_pipeline<double, kModeStiffness>(op, op->tab64, (const double*)u,
                                                 (double*)f, batch, spec,
-                                                (const double*)mat, st);
+                                                (const double*)mat, st, flags,
+                                                flag_stride);
   return run_pipeline<float, kModeStiffness>(op, op->tab32, (const float*)u,
                                              (float*)f, batch, spec,
-                                             (const float*)mat, st);
+                                             (const float*)mat, st, flags,
+                                             flag_stride);
 }
 
 int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,

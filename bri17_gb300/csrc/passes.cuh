@@ -25,6 +25,18 @@ constexpr int kThreads = 256;
 
 enum FusedMode { kModeStiffness = 0, kModeStrain = 1, kModeRhs = 2 };
 
+// Optional per-batch-entry mask: a CTA whose work belongs to entry z exits
+// at once when flags[z * stride] == 0.  `unit` is the number of CTA work
+// units (rows, outer lines) of one entry; null flags = every entry active.
+struct BatchMask {
+  const int* flags;
+  int stride;
+  int64_t unit;
+  __device__ __forceinline__ bool skip(int64_t first_unit) const {
+    return flags && flags[(first_unit / unit) * stride] == 0;
+  }
+};
+
 template <typename T>
 struct FusedParams {
   Tables<T> tab;
@@ -46,7 +58,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     rows_r2c(const T* __restrict__ x, cplx<T>* __restrict__ X, int64_t nrows,
              int n, int H, AxisPlan pm, const cplx<T>* __restrict__ tw_g,
-             int rows_per_cta, int pitch) {
+             int rows_per_cta, int pitch, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* a = tw + n;
@@ -54,6 +66,7 @@ __global__ void __launch_bounds__(kThreads)
   const bool even = (n % 2) == 0;
   const int m = even ? n / 2 : n;
   const int64_t row0 = (int64_t)blockIdx.x * rows_per_cta;
+  if (mask.skip(row0)) return;
   const int nr = (int)min((int64_t)rows_per_cta, nrows - row0);
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
   if (even) {
@@ -95,7 +108,7 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     rows_c2r(const cplx<T>* __restrict__ X, T* __restrict__ x, int64_t nrows,
              int n, int H, AxisPlan pm, const cplx<T>* __restrict__ tw_g,
-             int rows_per_cta, int pitch) {
+             int rows_per_cta, int pitch, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* a = tw + n;
@@ -103,6 +116,7 @@ __global__ void __launch_bounds__(kThreads)
   const bool even = (n % 2) == 0;
   const int m = even ? n / 2 : n;
   const int64_t row0 = (int64_t)blockIdx.x * rows_per_cta;
+  if (mask.skip(row0)) return;
   const int nr = (int)min((int64_t)rows_per_cta, nrows - row0);
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
   __syncthreads();
@@ -159,11 +173,12 @@ __global__ void __launch_bounds__(kThreads)
 template <typename T, bool INV>
 __global__ void __launch_bounds__(kThreads)
     axis_c2c(cplx<T>* __restrict__ X, int n, int64_t B, int TB, int pitch,
-             AxisPlan p, const cplx<T>* __restrict__ tw_g) {
+             AxisPlan p, const cplx<T>* __restrict__ tw_g, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* a = tw + n;
   cplx<T>* b = a + TB * pitch;
+  if (mask.skip(blockIdx.y)) return;
   const int64_t b0 = (int64_t)blockIdx.x * TB;
   const int nb = (int)min((int64_t)TB, B - b0);
   cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b0;
@@ -269,7 +284,7 @@ template <typename T, int DIM, int MODE>
 __global__ void __launch_bounds__(kThreads)
     axis0_fused(cplx<T>* __restrict__ X, int n0, int64_t P, int64_t cstride,
                 int64_t bstride, int TB, int pitch, AxisPlan p0,
-                FusedParams<T> fp) {
+                FusedParams<T> fp, BatchMask mask) {
   constexpr int SYM = DIM == 2 ? 3 : 6;
   constexpr int CIN = MODE == kModeRhs ? SYM : DIM;
   constexpr int COUT = MODE == kModeStrain ? SYM : DIM;
@@ -277,6 +292,7 @@ __global__ void __launch_bounds__(kThreads)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + n0;  // CMAX + 1 buffers of TB * pitch
+  if (mask.skip(blockIdx.y)) return;
   const int64_t b0 = (int64_t)blockIdx.x * TB;
   const int nb = (int)min((int64_t)TB, P - b0);
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b0;

@@ -1,19 +1,770 @@
-// server.cu -- continuous-batching solve server (placeholder until the
-// scheduler lands; every entry point reports BRI17_ERR_INVALID_ARGUMENT).
-#include "op.cuh"
+// server.cu -- continuous-batching server of periodic eigenstress solves.
+//
+// New (no reference counterpart; the reference solves one mode at a time,
+// include/bri17/bri17.hpp:308-355 driven by the Python loop of
+// python/demo.py:34-40).
+//
+// Requests are grouped by geometry (shape, L) into buckets.  A bucket owns
+// S slots of device vectors and runs ONE batched mixed-precision CG over all
+// its slots: every iteration is one batched FP32 operator application (the
+// five FFT passes cover all slots; per-slot materials come from a device
+// table) plus batched vector kernels with per-slot scalars, and a chunk of
+// iterations is replayed as a CUDA graph.  Converged or empty slots are
+// masked on the device (their CTAs exit at once), so requests that arrive
+// while others run are admitted into free slots without re-capturing.
+// Each bucket has its own stream; all buckets' graphs are launched before
+// any is waited on, so their work overlaps on the GPU.
+//
+// Per request (FP64 outer loop, as bri17_cg_solve's mixed mode): b = RHS(tau),
+// x = 0; repeat { r = b - K x (FP64), zero-mean projection, stop if
+// ||r|| <= tol ||b||; inner FP32 CG on K d = r / ||r||; x += ||r|| d }.
+// Admission is by device footprint: a new bucket is created only while the
+// server's total allocation stays within its memory budget.
+#include <math.h>
+#include <string.h>
 
-extern "C" int bri17_server_create(int64_t, int, bri17_server** s) {
-  if (s) *s = nullptr;
-  return BRI17_ERR_INVALID_ARGUMENT;
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <unordered_map>
+#include <vector>
+
+#include "op.cuh"
+#include "reduce.cuh"
+
+namespace bri17gb {
+namespace {
+
+constexpr int kSrvChunk = 16;  // inner iterations per graph replay
+
+struct Request {
+  int64_t id;
+  int shape[3];
+  double L[3];
+  double mu, nu;
+  std::vector<double> tau;  // 6 x size
+  double* x_host;
+  double tol;
+  int max_iterations;
+  double t_submit = 0, t_admit = 0, t_finish = 0;
+  int iters = 0, outer = 0;
+  double bb = 0, rel = 1, nr = 0;
+  int status = BRI17_OK;
+  bool cancel = false;
+};
+
+enum SlotState { kFree = 0, kInner = 1 };
+
+struct Bucket {
+  int shape[3];
+  double L[3];
+  int S = 0;
+  int64_t size = 0, n = 0;
+  bri17_op* op32 = nullptr;
+  bri17_op* op64 = nullptr;
+  double *b = nullptr, *x = nullptr, *r = nullptr, *q64 = nullptr, *tau = nullptr;
+  float *d = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  float* mat32 = nullptr;
+  double* mat64 = nullptr;
+  void* spec32 = nullptr;
+  CgState* st = nullptr;
+  CgState* st_host = nullptr;
+  double* partials = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<int> slot_state;
+  std::vector<Request*> slot_req;
+  int64_t bytes = 0;
+  bool launched = false;
+};
+
+// --- batched CG kernels: grid (blocks, S), slot z = blockIdx.y -----------
+
+__device__ __forceinline__ double slot_block_total(double v, double* partials,
+                                                   unsigned int* counter,
+                                                   int nparts, double* total,
+                                                   bool* last) {
+  __shared__ bool is_last;
+  const double b = block_sum(v);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b;
+    __threadfence();
+    const unsigned int t = atomicAdd(counter, 1u);
+    is_last = (t == (unsigned int)nparts - 1);
+  }
+  __syncthreads();
+  *last = is_last;
+  if (!is_last) return 0.0;
+  __threadfence();
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += __ldcg(partials + i);
+  const double tot = block_sum(s);
+  if (threadIdx.x == 0) {
+    *total = tot;
+    *counter = 0u;
+  }
+  return tot;
 }
-extern "C" int bri17_server_destroy(bri17_server*) { return BRI17_OK; }
-extern "C" int bri17_server_submit(bri17_server*, const int*, const double*, double, double,
-                                   const double*, double*, double, int, int64_t*) {
-  return BRI17_ERR_INVALID_ARGUMENT;
+
+__global__ void __launch_bounds__(kRedThreads)
+    kb_dot_pq(const float* __restrict__ p, const float* __restrict__ q, int64_t n,
+              CgState* sts, double* partials) {
+  CgState* st = sts + blockIdx.y;
+  if (!st->active) return;
+  const float* pz = p + blockIdx.y * n;
+  const float* qz = q + blockIdx.y * n;
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v += (double)pz[i] * (double)qz[i];
+  double tot;
+  bool last;
+  slot_block_total(v, partials + blockIdx.y * kRedMaxBlocks, &st->counter, gridDim.x,
+                   &tot, &last);
+  if (last && threadIdx.x == 0) {
+    st->pq = tot;
+    if (!(tot > 0.0) || !isfinite(tot)) {
+      st->flag = BRI17_ERR_BREAKDOWN;
+      st->active = 0;
+    } else {
+      st->alpha = st->rr / tot;
+    }
+  }
 }
-extern "C" int bri17_server_step(bri17_server*, int*) { return BRI17_ERR_INVALID_ARGUMENT; }
-extern "C" int bri17_server_poll(bri17_server*, bri17_request_result*, int, int*) {
-  return BRI17_ERR_INVALID_ARGUMENT;
+
+__global__ void __launch_bounds__(kRedThreads)
+    kb_update(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+              const float* __restrict__ q, int64_t n, CgState* sts, double* partials,
+              int max_iters) {
+  CgState* st = sts + blockIdx.y;
+  if (!st->active) return;
+  const int64_t o = blockIdx.y * n;
+  const float a = (float)st->alpha;
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[o + i] += a * p[o + i];
+    const float ri = r[o + i] - a * q[o + i];
+    r[o + i] = ri;
+    v += (double)ri * (double)ri;
+  }
+  double tot;
+  bool last;
+  slot_block_total(v, partials + blockIdx.y * kRedMaxBlocks, &st->counter, gridDim.x,
+                   &tot, &last);
+  if (last && threadIdx.x == 0) {
+    st->iters += 1;
+    if (!isfinite(tot)) {
+      st->flag = BRI17_ERR_BREAKDOWN;
+      st->active = 0;
+      return;
+    }
+    st->beta = tot / st->rr;
+    st->rr = tot;
+    if (tot <= st->thresh || st->iters >= max_iters) st->active = 0;
+  }
 }
-extern "C" int bri17_server_cancel(bri17_server*, int64_t) { return BRI17_ERR_INVALID_ARGUMENT; }
-extern "C" double bri17_server_clock(const bri17_server*) { return 0.0; }
+
+__global__ void __launch_bounds__(kRedThreads)
+    kb_pupdate(float* __restrict__ p, const float* __restrict__ r, int64_t n,
+               const CgState* sts) {
+  const CgState* st = sts + blockIdx.y;
+  if (!st->active) return;
+  const int64_t o = blockIdx.y * n;
+  const float b = (float)st->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[o + i] = r[o + i] + b * p[o + i];
+}
+
+// --- per-slot helpers (one slot, 1-D grids) --------------------------------
+
+__global__ void __launch_bounds__(kRedThreads)
+    ks_dot(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+           CgState* st, double* partials) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v += a[i] * b[i];
+  double tot;
+  bool last;
+  slot_block_total(v, partials, &st->counter, gridDim.x, &tot, &last);
+  if (last && threadIdx.x == 0) st->aux = tot;
+}
+
+// r = b - kx, then subtract per-component means computed in a second kernel.
+__global__ void ks_residual(double* __restrict__ r, const double* __restrict__ b,
+                            const double* __restrict__ kx, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = b[i] - kx[i];
+}
+
+__global__ void __launch_bounds__(kRedThreads)
+    ks_comp_mean(const double* __restrict__ a, int64_t size, CgState* st,
+                 double* partials) {
+  const double* ac = a + (int64_t)blockIdx.y * size;
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < size;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v += ac[i];
+  __shared__ bool is_last;
+  const double b = block_sum(v);
+  const int nparts = gridDim.x * gridDim.y;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x + blockIdx.y * gridDim.x] = b;
+    __threadfence();
+    const unsigned int t = atomicAdd(&st->counter, 1u);
+    is_last = (t == (unsigned int)nparts - 1);
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int c = 0; c < (int)gridDim.y; c++) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      s += __ldcg(partials + c * gridDim.x + i);
+    const double tot = block_sum(s);
+    if (threadIdx.x == 0) st->mean[c] = tot / (double)size;
+  }
+  if (threadIdx.x == 0) st->counter = 0u;
+}
+
+__global__ void ks_sub_mean(double* __restrict__ a, int64_t size, const CgState* st) {
+  const double m = st->mean[blockIdx.y];
+  double* ac = a + (int64_t)blockIdx.y * size;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < size;
+       i += (int64_t)gridDim.x * blockDim.x)
+    ac[i] -= m;
+}
+
+// Inner CG restart: r32 = r * scale, d = 0, p = r32, rr, thresh, active.
+__global__ void __launch_bounds__(kRedThreads)
+    ks_restart(const double* __restrict__ r, double scale, float* __restrict__ r32,
+               float* __restrict__ d, float* __restrict__ p, int64_t n, CgState* st,
+               double* partials, double tin2) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float ri = (float)(r[i] * scale);
+    r32[i] = ri;
+    p[i] = ri;
+    d[i] = 0.f;
+    v += (double)ri * (double)ri;
+  }
+  double tot;
+  bool last;
+  slot_block_total(v, partials, &st->counter, gridDim.x, &tot, &last);
+  if (last && threadIdx.x == 0) {
+    st->rr = tot;
+    st->thresh = tin2 * tot;
+    st->iters = 0;
+    st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
+    st->active = (tot > st->thresh && isfinite(tot)) ? 1 : 0;
+  }
+}
+
+__global__ void ks_axpy32(double* __restrict__ x, const float* __restrict__ d, double a,
+                          int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += a * (double)d[i];
+}
+
+__global__ void ks_set_inactive(CgState* st) { st->active = 0; }
+
+unsigned g1(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+}  // namespace bri17gb
+
+using namespace bri17gb;
+
+struct bri17_server {
+  int64_t budget = 0;
+  int max_active = 8;  // slots per bucket
+  int64_t used = 0;
+  int64_t next_id = 1;
+  std::deque<Request*> queue;
+  std::vector<Bucket*> buckets;
+  std::vector<bri17_request_result> done;
+  std::unordered_map<int64_t, Request*> live;
+  std::chrono::steady_clock::time_point t0;
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace {
+
+#define SRV_TRY(expr)                                   \
+  do {                                                  \
+    cudaError_t _e = (expr);                            \
+    if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
+  } while (0)
+
+int64_t slot_bytes(int64_t n) { return n * (5 * 8 + 4 * 4); }
+
+int64_t bucket_bytes(const int* shape, int S) {
+  int64_t size = (int64_t)shape[0] * shape[1] * shape[2];
+  int64_t n = 3 * size;
+  int64_t cspec = (int64_t)shape[0] * shape[1] * (shape[2] / 2 + 1);
+  return S * slot_bytes(n) + 6 * size * 8 /* tau staging */ +
+         (int64_t)S * 3 * cspec * 8 /* FP32 batched spectrum */ +
+         6 * cspec * 16 + 3 * cspec * 8 /* op64 / op32 own spectra */ +
+         (int64_t)S * (kRedMaxBlocks * 8 + sizeof(CgState));
+}
+
+void free_bucket(Bucket* B) {
+  if (!B) return;
+  if (B->stream) cudaStreamSynchronize(B->stream);
+  if (B->graph) cudaGraphExecDestroy(B->graph);
+  bri17_op_destroy(B->op32);
+  bri17_op_destroy(B->op64);
+  void* ps[] = {B->b, B->x, B->r, B->q64, B->tau, B->d, B->r32, B->p32, B->q32,
+                B->mat32, B->mat64, B->spec32, B->st, B->partials};
+  for (void* p : ps) cudaFree(p);
+  cudaFreeHost(B->st_host);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+}
+
+int capture_graph(Bucket* B) {
+  const int64_t n = B->n;
+  const int rb = red_blocks(n);
+  cudaStream_t s = B->stream;
+  cudaGraph_t g;
+  SRV_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = BRI17_OK;
+  const int flag_stride = (int)(sizeof(CgState) / sizeof(int));
+  const int* flags = &B->st[0].active;
+  for (int it = 0; it < kSrvChunk && rc == BRI17_OK; it++) {
+    rc = apply_stiffness_batched_async(B->op32, B->S, B->p32, B->q32, B->spec32, B->mat32, s,
+                                       flags, flag_stride);
+    dim3 grid(rb, B->S);
+    kb_dot_pq<<<grid, kRedThreads, 0, s>>>(B->p32, B->q32, n, B->st, B->partials);
+    kb_update<<<grid, kRedThreads, 0, s>>>(B->d, B->r32, B->p32, B->q32, n, B->st,
+                                           B->partials, 1 << 30);
+    dim3 g2(g1(n), B->S);
+    kb_pupdate<<<g2, 256, 0, s>>>(B->p32, B->r32, n, B->st);
+  }
+  cudaMemcpyAsync(B->st_host, B->st, B->S * sizeof(CgState), cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (rc != BRI17_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&B->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  return BRI17_OK;
+}
+
+int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
+  // The axis-1 pass launches S * 3 * n0 CTA rows (grid.y <= 65535).
+  const int S = std::max(1, std::min(srv->max_active, 65535 / (3 * q->shape[0])));
+  const int64_t bytes = bucket_bytes(q->shape, S);
+  if (srv->used + bytes > srv->budget) return BRI17_ERR_BUSY;
+  Bucket* B = new Bucket();
+  memcpy(B->shape, q->shape, sizeof(B->shape));
+  memcpy(B->L, q->L, sizeof(B->L));
+  B->S = S;
+  B->size = (int64_t)q->shape[0] * q->shape[1] * q->shape[2];
+  B->n = 3 * B->size;
+  B->bytes = bytes;
+  auto fail = [&](int rc) {
+    free_bucket(B);
+    return rc;
+  };
+  int rc = bri17_op_create(3, q->shape, q->L, 1.0, 0.3, BRI17_F32, &B->op32);
+  if (rc != BRI17_OK) return fail(rc);
+  rc = bri17_op_create(3, q->shape, q->L, 1.0, 0.3, BRI17_F64, &B->op64);
+  if (rc != BRI17_OK) return fail(rc);
+  rc = ensure_spectrum(B->op64, 6);
+  if (rc != BRI17_OK) return fail(rc);
+  const int64_t n = B->n, Sn = S * n;
+  const int64_t cspec = B->op32->g.cspec;
+#define ALLOC(p, bytes_)                                                   \
+  do {                                                                     \
+    cudaError_t _e = cudaMalloc((void**)&(p), (bytes_));                   \
+    if (_e != cudaSuccess) return fail(cuda_fail(_e, "cudaMalloc(bucket)")); \
+  } while (0)
+  ALLOC(B->b, Sn * 8);
+  ALLOC(B->x, Sn * 8);
+  ALLOC(B->r, Sn * 8);
+  ALLOC(B->q64, Sn * 8);
+  ALLOC(B->tau, 6 * B->size * 8);
+  ALLOC(B->d, Sn * 4);
+  ALLOC(B->r32, Sn * 4);
+  ALLOC(B->p32, Sn * 4);
+  ALLOC(B->q32, Sn * 4);
+  ALLOC(B->mat32, S * 2 * 4);
+  ALLOC(B->mat64, S * 2 * 8);
+  ALLOC(B->spec32, (int64_t)S * 3 * cspec * 8);
+  ALLOC(B->st, S * sizeof(CgState));
+  ALLOC(B->partials, (int64_t)S * kRedMaxBlocks * 8);
+#undef ALLOC
+  if (cudaMallocHost((void**)&B->st_host, S * sizeof(CgState)) != cudaSuccess)
+    return fail(cuda_fail(cudaErrorMemoryAllocation, "cudaMallocHost"));
+  memset(B->st_host, 0, S * sizeof(CgState));
+  if (cudaMemset(B->st, 0, S * sizeof(CgState)) != cudaSuccess ||
+      cudaMemset(B->mat32, 0, S * 2 * 4) != cudaSuccess ||
+      cudaMemset(B->mat64, 0, S * 2 * 8) != cudaSuccess ||
+      cudaMemset(B->p32, 0, Sn * 4) != cudaSuccess)
+    return fail(cuda_fail(cudaErrorUnknown, "cudaMemset(bucket)"));
+  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(cuda_fail(cudaErrorUnknown, "cudaStreamCreate"));
+  B->slot_state.assign(S, kFree);
+  B->slot_req.assign(S, nullptr);
+  rc = capture_graph(B);
+  if (rc != BRI17_OK) return fail(rc);
+  srv->used += bytes;
+  srv->buckets.push_back(B);
+  *out = B;
+  return BRI17_OK;
+}
+
+Bucket* find_bucket(bri17_server* srv, const Request* q) {
+  for (Bucket* B : srv->buckets)
+    if (memcmp(B->shape, q->shape, sizeof(B->shape)) == 0 &&
+        memcmp(B->L, q->L, sizeof(B->L)) == 0)
+      return B;
+  return nullptr;
+}
+
+int free_slot(const Bucket* B) {
+  for (int z = 0; z < B->S; z++)
+    if (B->slot_state[z] == kFree) return z;
+  return -1;
+}
+
+// Enqueue the FP64 outer residual of slot z: r = b - K x, projected, and
+// aux = r.r (read by the caller after a sync).
+int enqueue_residual(Bucket* B, int z, bool x_is_zero) {
+  const int64_t n = B->n;
+  cudaStream_t s = B->stream;
+  double* bz = B->b + z * n;
+  double* xz = B->x + z * n;
+  double* rz = B->r + z * n;
+  CgState* st = B->st + z;
+  double* parts = B->partials + z * kRedMaxBlocks;
+  if (x_is_zero) {
+    SRV_TRY(cudaMemcpyAsync(rz, bz, n * 8, cudaMemcpyDeviceToDevice, s));
+  } else {
+    dim3 gm(std::min(red_blocks(B->size), kRedMaxBlocks / 3), 3);
+    ks_comp_mean<<<gm, kRedThreads, 0, s>>>(xz, B->size, st, parts);
+    ks_sub_mean<<<dim3(g1(B->size), 3), 256, 0, s>>>(xz, B->size, st);
+    int rc = apply_stiffness_batched_async(B->op64, 1, xz, B->q64 + z * n, B->op64->spec,
+                                           B->mat64 + 2 * z, s);
+    if (rc != BRI17_OK) return rc;
+    ks_residual<<<g1(n), 256, 0, s>>>(rz, bz, B->q64 + z * n, n);
+  }
+  dim3 gm(std::min(red_blocks(B->size), kRedMaxBlocks / 3), 3);
+  ks_comp_mean<<<gm, kRedThreads, 0, s>>>(rz, B->size, st, parts);
+  ks_sub_mean<<<dim3(g1(B->size), 3), 256, 0, s>>>(rz, B->size, st);
+  ks_dot<<<red_blocks(n), kRedThreads, 0, s>>>(rz, rz, n, st, parts);
+  SRV_TRY(cudaMemcpyAsync(&B->st_host[z], st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+  return BRI17_OK;
+}
+
+void finish(bri17_server* srv, Request* q, int status) {
+  q->status = status;
+  q->t_finish = srv->now();
+  bri17_request_result res;
+  res.id = q->id;
+  res.status = status;
+  res.iterations = q->iters;
+  res.outer_iterations = q->outer;
+  res.rel_residual = q->rel;
+  res.submit_time_s = q->t_submit;
+  res.admit_time_s = q->t_admit;
+  res.finish_time_s = q->t_finish;
+  srv->done.push_back(res);
+  srv->live.erase(q->id);
+  delete q;
+}
+
+// Admit q into slot z of B: upload tau and material, compute b, start the
+// outer loop (x = 0, r = b).
+int admit(bri17_server* srv, Bucket* B, int z, Request* q) {
+  cudaStream_t s = B->stream;
+  const int64_t n = B->n;
+  q->t_admit = srv->now();
+  SRV_TRY(cudaMemcpyAsync(B->tau, q->tau.data(), 6 * B->size * 8, cudaMemcpyHostToDevice, s));
+  const double corr = B->op64->corr;
+  const double scaling = q->mu / (1. - 2. * q->nu);
+  const double m64[2] = {scaling * corr, q->mu * corr};
+  const float m32[2] = {(float)m64[0], (float)m64[1]};
+  SRV_TRY(cudaMemcpyAsync(B->mat64 + 2 * z, m64, sizeof(m64), cudaMemcpyHostToDevice, s));
+  SRV_TRY(cudaMemcpyAsync(B->mat32 + 2 * z, m32, sizeof(m32), cudaMemcpyHostToDevice, s));
+  int rc = eigenstress_rhs_batched_async(B->op64, 1, B->tau, B->b + z * n, B->op64->spec, s);
+  if (rc != BRI17_OK) return rc;
+  SRV_TRY(cudaMemsetAsync(B->x + z * n, 0, n * 8, s));
+  // The pageable tau copy has been staged when cudaMemcpyAsync returned; the
+  // host copy can go.
+  std::vector<double>().swap(q->tau);
+  rc = enqueue_residual(B, z, true);
+  if (rc != BRI17_OK) return rc;
+  SRV_TRY(cudaStreamSynchronize(s));
+  q->bb = B->st_host[z].aux;
+  B->slot_state[z] = kInner;
+  B->slot_req[z] = q;
+  return BRI17_OK;
+}
+
+// Outer step of slot z after its residual is known (st_host[z].aux = r.r):
+// retire or restart the inner CG.  Returns true if the slot stays busy.
+int outer_decide(bri17_server* srv, Bucket* B, int z, bool* busy) {
+  Request* q = B->slot_req[z];
+  const double rr = B->st_host[z].aux;
+  *busy = false;
+  if (!isfinite(rr) || !isfinite(q->bb)) {
+    q->rel = NAN;
+    B->slot_state[z] = kFree;
+    B->slot_req[z] = nullptr;
+    finish(srv, q, BRI17_ERR_BREAKDOWN);
+    return BRI17_OK;
+  }
+  q->rel = q->bb > 0 ? sqrt(rr / q->bb) : 0.0;
+  const bool converged = q->rel <= q->tol || q->bb == 0.0;
+  if (converged || q->iters >= q->max_iterations || q->cancel) {
+    const int64_t n = B->n;
+    SRV_TRY(cudaMemcpyAsync(q->x_host, B->x + z * n, n * 8, cudaMemcpyDeviceToHost,
+                            B->stream));
+    SRV_TRY(cudaStreamSynchronize(B->stream));
+    B->slot_state[z] = kFree;
+    B->slot_req[z] = nullptr;
+    finish(srv, q, q->cancel ? BRI17_ERR_CANCELLED
+                             : converged ? BRI17_OK : BRI17_ERR_NOT_CONVERGED);
+    return BRI17_OK;
+  }
+  double tin = 0.1 * q->tol / q->rel;
+  if (tin < 1e-5) tin = 1e-5;
+  if (tin > 1e-2) tin = 1e-2;
+  q->nr = sqrt(rr);
+  q->outer += 1;
+  const int64_t n = B->n;
+  ks_restart<<<red_blocks(n), kRedThreads, 0, B->stream>>>(
+      B->r + z * n, 1.0 / q->nr, B->r32 + z * n, B->d + z * n, B->p32 + z * n, n, B->st + z,
+      B->partials + z * kRedMaxBlocks, tin * tin);
+  *busy = true;
+  return BRI17_OK;
+}
+
+}  // namespace
+
+extern "C" int bri17_server_create(int64_t budget, int max_active, bri17_server** out) {
+  if (!out) {
+    set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  *out = nullptr;
+  if (budget <= 0 || max_active < 1 || max_active > 64) {
+    set_error("memory budget must be > 0 and max_active in [1, 64]");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device visible");
+    return BRI17_ERR_NO_DEVICE;
+  }
+  bri17_server* s = new bri17_server();
+  s->budget = budget;
+  s->max_active = max_active;
+  s->t0 = std::chrono::steady_clock::now();
+  *out = s;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_server_destroy(bri17_server* srv) {
+  if (!srv) return BRI17_OK;
+  for (Bucket* B : srv->buckets) free_bucket(B);
+  for (Request* q : srv->queue) delete q;
+  for (auto& kv : srv->live)
+    if (std::find(srv->queue.begin(), srv->queue.end(), kv.second) == srv->queue.end())
+      delete kv.second;
+  delete srv;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_server_submit(bri17_server* srv, const int* shape, const double* L,
+                                   double mu, double nu, const double* tau_host,
+                                   double* x_host, double tol, int max_iterations,
+                                   int64_t* id) {
+  if (!srv || !shape || !L || !tau_host || !x_host || !id) {
+    set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  for (int i = 0; i < 3; i++)
+    if (shape[i] < 1 || shape[i] > 1024 || !(L[i] > 0)) {
+      set_error("shape entries must be in [1, 1024] and L entries positive");
+      return BRI17_ERR_INVALID_ARGUMENT;
+    }
+  if (!(mu > 0) || !(nu > -1.0 && nu < 0.5) || !(tol > 0) || max_iterations < 1) {
+    set_error("need mu > 0, -1 < nu < 0.5, tol > 0, max_iterations >= 1");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  AxisPlan p;
+  for (int i = 0; i < 3; i++)
+    if (!make_plan(shape[i], &p)) {
+      set_error("axis length has a prime factor above 61");
+      return BRI17_ERR_UNSUPPORTED_SIZE;
+    }
+  if (bucket_bytes(shape, 1) > srv->budget) {
+    set_error("request footprint exceeds the server's memory budget");
+    return BRI17_ERR_OUT_OF_MEMORY;
+  }
+  Request* q = new Request();
+  q->id = srv->next_id++;
+  memcpy(q->shape, shape, sizeof(q->shape));
+  memcpy(q->L, L, sizeof(q->L));
+  q->mu = mu;
+  q->nu = nu;
+  const int64_t size = (int64_t)shape[0] * shape[1] * shape[2];
+  q->tau.assign(tau_host, tau_host + 6 * size);
+  q->x_host = x_host;
+  q->tol = tol;
+  q->max_iterations = max_iterations;
+  q->t_submit = srv->now();
+  srv->queue.push_back(q);
+  srv->live[q->id] = q;
+  *id = q->id;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_server_cancel(bri17_server* srv, int64_t id) {
+  if (!srv) {
+    set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  auto it = srv->live.find(id);
+  if (it == srv->live.end()) return BRI17_ERR_NOT_FOUND;
+  Request* q = it->second;
+  for (auto qi = srv->queue.begin(); qi != srv->queue.end(); ++qi)
+    if (*qi == q) {
+      srv->queue.erase(qi);
+      finish(srv, q, BRI17_ERR_CANCELLED);
+      return BRI17_OK;
+    }
+  q->cancel = true;  // running: retired at the next step
+  return BRI17_OK;
+}
+
+extern "C" int bri17_server_step(bri17_server* srv, int* active) {
+  if (!srv) {
+    set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  // 1. Admission: FIFO, skipping requests whose bucket is full (no
+  //    head-of-line blocking across geometries).
+  for (auto it = srv->queue.begin(); it != srv->queue.end();) {
+    Request* q = *it;
+    Bucket* B = find_bucket(srv, q);
+    if (!B) {
+      int rc = make_bucket(srv, q, &B);
+      if (rc == BRI17_ERR_BUSY) {
+        // Release an idle bucket of another geometry, then retry once.
+        for (size_t i = 0; i < srv->buckets.size(); i++) {
+          Bucket* E = srv->buckets[i];
+          bool idle = true;
+          for (int z = 0; z < E->S; z++) idle = idle && E->slot_state[z] == kFree;
+          if (idle) {
+            srv->used -= E->bytes;
+            free_bucket(E);
+            srv->buckets.erase(srv->buckets.begin() + i);
+            break;
+          }
+        }
+        rc = make_bucket(srv, q, &B);
+      }
+      if (rc == BRI17_ERR_BUSY) {
+        ++it;
+        continue;
+      }
+      if (rc != BRI17_OK) return rc;
+    }
+    const int z = free_slot(B);
+    if (z < 0) {
+      ++it;
+      continue;
+    }
+    it = srv->queue.erase(it);
+    int rc = admit(srv, B, z, q);
+    if (rc != BRI17_OK) return rc;
+    bool busy;
+    rc = outer_decide(srv, B, z, &busy);
+    if (rc != BRI17_OK) return rc;
+  }
+  // 2. One graph replay per bucket with work, all launched before any wait.
+  for (Bucket* B : srv->buckets) {
+    B->launched = false;
+    for (int z = 0; z < B->S; z++)
+      if (B->slot_state[z] == kInner) B->launched = true;
+    if (B->launched) SRV_TRY(cudaGraphLaunch(B->graph, B->stream));
+  }
+  // 3. Outer steps of slots whose inner CG finished (or were cancelled).
+  for (Bucket* B : srv->buckets) {
+    if (!B->launched) continue;
+    SRV_TRY(cudaStreamSynchronize(B->stream));
+    std::vector<int> outer;
+    for (int z = 0; z < B->S; z++) {
+      if (B->slot_state[z] != kInner) continue;
+      Request* q = B->slot_req[z];
+      const CgState& h = B->st_host[z];
+      if (q->cancel && h.active) {
+        ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
+      }
+      if (!h.active || q->cancel) {
+        q->iters += h.iters;
+        if (h.flag != BRI17_OK && h.iters == 0) {
+          q->rel = NAN;
+          B->slot_state[z] = kFree;
+          B->slot_req[z] = nullptr;
+          finish(srv, q, BRI17_ERR_BREAKDOWN);
+          continue;
+        }
+        ks_axpy32<<<g1(B->n), 256, 0, B->stream>>>(B->x + z * B->n, B->d + z * B->n, q->nr,
+                                                   B->n);
+        int rc = enqueue_residual(B, z, false);
+        if (rc != BRI17_OK) return rc;
+        outer.push_back(z);
+      } else if (q->iters + h.iters >= q->max_iterations) {
+        ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
+      }
+    }
+    if (outer.empty()) continue;
+    SRV_TRY(cudaStreamSynchronize(B->stream));
+    for (int z : outer) {
+      bool busy;
+      int rc = outer_decide(srv, B, z, &busy);
+      if (rc != BRI17_OK) return rc;
+    }
+  }
+  int n_active = 0;
+  for (Bucket* B : srv->buckets)
+    for (int z = 0; z < B->S; z++) n_active += B->slot_state[z] == kInner;
+  if (active) *active = n_active;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "server step");
+  return BRI17_OK;
+}
+
+extern "C" int bri17_server_poll(bri17_server* srv, bri17_request_result* out, int cap,
+                                 int* count) {
+  if (!srv || (!out && cap > 0) || !count) {
+    set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  const int k = (int)std::min<size_t>(cap, srv->done.size());
+  for (int i = 0; i < k; i++) out[i] = srv->done[i];
+  srv->done.erase(srv->done.begin(), srv->done.begin() + k);
+  *count = k;
+  return BRI17_OK;
+}
+
+extern "C" double bri17_server_clock(const bri17_server* srv) {
+  return srv ? srv->now() : 0.0;
+}

@@ -1,0 +1,104 @@
+"""Continuous-batching server: every result equals its solo solve within
+the stated tolerance (both are solved to 1e-8 relative residual, so they
+agree to kappa * 1e-8 with the exact oracle solution), requests are admitted
+while others run, cancellation and validation behave."""
+import numpy as np
+import pytest
+
+from gpu_helpers import pair, rel_l2, to_dev
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8
+SOLUTION_TOL = 1e-5  # kappa (< 1e3 on these grids) * TOL, with margin
+
+
+def _requests(rng, n, sides):
+    reqs = []
+    for i in range(n):
+        s = sides[i % len(sides)]
+        shape = (s, s, s) if isinstance(s, int) else s
+        mu = float(rng.uniform(0.5, 2.0))
+        nu = float(rng.uniform(0.1, 0.45))
+        tau = rng.standard_normal((6,) + shape)
+        reqs.append((shape, (1.0, 1.0, 1.0), mu, nu, tau))
+    return reqs
+
+
+def test_server_results_equal_solo_solves_and_oracle():
+    from bri17_gb300.server import Server
+    rng = np.random.default_rng(3)
+    reqs = _requests(rng, 9, [16, 24, (20, 16, 12)])
+    srv = Server(memory_budget_bytes=2 << 30, slots_per_bucket=4)
+    ids = [srv.submit(*r, tol=TOL) for r in reqs]
+    results = {r["id"]: r for r in srv.run_until_idle()}
+    assert sorted(results) == sorted(ids)
+    for rid, (shape, L, mu, nu, tau) in zip(ids, reqs):
+        res = results[rid]
+        assert res["status"] == 0, res
+        assert res["rel_residual"] <= TOL
+        x_srv = srv.result(rid)
+        h, ho = pair(shape, L, mu, nu)
+        b = h.eigenstress_rhs(to_dev(tau))
+        x_solo, info = h.cg_solve(b, tol=TOL, mode="mixed")
+        x_ref = O.eigenstress_solve(ho, tau)
+        assert rel_l2(x_srv, x_solo.cpu().numpy()) <= SOLUTION_TOL
+        assert rel_l2(x_srv, x_ref) <= SOLUTION_TOL
+        # True FP64 residual of the served solution.
+        r = b - h.apply_stiffness(to_dev(x_srv))
+        assert float(r.norm() / b.norm()) <= 1.01 * TOL
+    srv.close()
+
+
+def test_requests_are_admitted_while_others_run():
+    """Two slots, five requests of one size: later requests enter slots freed
+    by earlier ones while the other slot is still solving."""
+    from bri17_gb300.server import Server
+    rng = np.random.default_rng(4)
+    reqs = _requests(rng, 5, [16])
+    srv = Server(memory_budget_bytes=1 << 30, slots_per_bucket=2)
+    ids = [srv.submit(*r, tol=TOL) for r in reqs]
+    results = {r["id"]: r for r in srv.run_until_idle()}
+    assert all(results[i]["status"] == 0 for i in ids)
+    admits = sorted(results[i]["admit_time_s"] for i in ids)
+    finishes = sorted(results[i]["finish_time_s"] for i in ids)
+    # The third admission happens after the first finish and before the last.
+    assert admits[2] >= finishes[0] and admits[2] < finishes[-1]
+    overlap = any(results[a]["admit_time_s"] < results[b]["finish_time_s"] and
+                  results[b]["admit_time_s"] < results[a]["finish_time_s"]
+                  for a in ids for b in ids if a != b)
+    assert overlap
+    srv.close()
+
+
+def test_cancel_queued_and_running():
+    from bri17_gb300.server import Server
+    rng = np.random.default_rng(5)
+    reqs = _requests(rng, 3, [24])
+    srv = Server(memory_budget_bytes=1 << 30, slots_per_bucket=1)
+    ids = [srv.submit(*r, tol=1e-12, max_iterations=100000) for r in reqs]
+    srv.step()                      # first request admitted and running
+    assert srv.cancel(ids[2]) == 0  # still queued
+    assert srv.cancel(ids[0]) == 0  # running
+    assert srv.cancel(999999) == 9  # unknown id
+    results = {r["id"]: r for r in srv.run_until_idle()}
+    assert results[ids[2]]["status"] == 10
+    assert results[ids[0]]["status"] == 10
+    assert results[ids[1]]["status"] == 0
+    srv.close()
+
+
+def test_submit_validation():
+    from bri17_gb300._lib import Bri17Error
+    from bri17_gb300.server import Server
+    srv = Server(memory_budget_bytes=64 << 20, slots_per_bucket=2)
+    tau = np.zeros((6, 8, 8, 8))
+    with pytest.raises(Bri17Error):
+        srv.submit((8, 8, 8), (1, 1, 1), 1.0, 0.5, tau)      # nu = 0.5
+    with pytest.raises(Bri17Error):
+        srv.submit((256, 256, 256), (1, 1, 1), 1.0, 0.3, np.zeros(6 * 256 ** 3))
+    rid = srv.submit((8, 8, 8), (1, 1, 1), 1.0, 0.3, tau)  # tau = 0 -> x = 0
+    res = srv.run_until_idle()
+    assert res[0]["status"] == 0 and np.all(srv.result(rid) == 0)
+    srv.close()
