@@ -8,6 +8,7 @@
 
 #include "../../include/bri17_gb300.h"
 #include "fft.cuh"
+#include "fft8.cuh"
 
 namespace bri17gb {
 
@@ -49,7 +50,20 @@ struct Geometry {
   int64_t cspec;   // complex spectrum entries per component (n[0] * P)
   AxisPlan plan_row;  // last axis: length n/2 (even n) or n (odd n)
   AxisPlan plan[3];   // full-length plans of each axis
+  // Register-resident plans for power-of-two lengths (fft8.cuh); a pass
+  // uses them when its flag is set, else the generic engine.
+  Plan8 p8_row;       // last axis, length n/2
+  Plan8 p8[3];
+  bool use_p8_row;
+  bool use_p8[3];
 };
+
+// Fill the register-resident plans of a geometry whose n, dim are set.
+inline void set_p8_plans(Geometry* g) {
+  const int nl = g->n[g->dim - 1];
+  g->use_p8_row = (nl % 2 == 0) && make_plan8(nl / 2, &g->p8_row);
+  for (int i = 0; i < 3; i++) g->use_p8[i] = i < g->dim && make_plan8(g->n[i], &g->p8[i]);
+}
 
 bool make_plan(int n, AxisPlan* p);
 

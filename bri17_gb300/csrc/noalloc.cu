@@ -170,6 +170,7 @@ extern "C" int bri17_apply_stiffness_noalloc(int dim, const int* shape, const do
   g.cspec = (int64_t)g.n[0] * g.P;
   bool ok = plan_fixed(nl % 2 == 0 ? nl / 2 : nl, &g.plan_row);
   for (int i = 0; i < dim; i++) ok = ok && plan_fixed(g.n[i], &g.plan[i]);
+  set_p8_plans(&g);
   if (!ok) return fail(BRI17_ERR_UNSUPPORTED_SIZE, "axis length has a prime factor above 61");
   const size_t tbytes = table_bytes(g.n, dim);
   const size_t spec_off = (tbytes + 255) & ~size_t(255);

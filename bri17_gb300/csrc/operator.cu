@@ -11,6 +11,7 @@
 
 #include "op.cuh"
 #include "passes.cuh"
+#include "passes_p2.cuh"
 
 namespace bri17gb {
 
@@ -182,6 +183,12 @@ static void set_smem_attrs() {
     cudaFuncSetAttribute(rows_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(axis_c2c<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(axis_c2c<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(rows_r2c_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(rows_c2r_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis_c2c_p2<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis_c2c_p2<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis0_stiffness_p2<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis0_stiffness_p2<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
 #define SET_FUSED(D, M) \
   cudaFuncSetAttribute(axis0_fused<T, D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem)
     SET_FUSED(2, kModeStiffness);
@@ -206,10 +213,27 @@ static int rows_per_cta(int m, int64_t nrows, int64_t rows_per_entry, bool maske
   return (int)r;
 }
 
+// Rows per CTA of the register-resident row passes: 256 threads' worth,
+// a power of two dividing the rows of one batch entry when masked.
+static int rows_p8(int T, int64_t nrows, int64_t unit, bool masked) {
+  int rb = kP2Threads / T;
+  if (masked)
+    while (rb > 1 && unit % rb != 0) rb /= 2;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(rb, nrows));
+}
+
 template <typename T>
 static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
                            int64_t nrows, const Tables<T>& tab, BatchMask mask,
                            cudaStream_t st) {
+  if (g.use_p8_row) {
+    const Plan8& p = g.p8_row;
+    const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
+    const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
+    rows_r2c_p2<T><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
+        x, X, nrows, g.H, p, tab.tw[g.dim - 1], rb, mask);
+    return BRI17_OK;
+  }
   const int n = g.n[g.dim - 1];
   const int m = (n % 2 == 0) ? n / 2 : n;
   const int pitch = m + 1;
@@ -225,6 +249,14 @@ template <typename T>
 static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
                            int64_t nrows, const Tables<T>& tab, BatchMask mask,
                            cudaStream_t st) {
+  if (g.use_p8_row) {
+    const Plan8& p = g.p8_row;
+    const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
+    const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
+    rows_c2r_p2<T><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
+        X, x, nrows, g.H, p, tab.tw[g.dim - 1], rb, mask);
+    return BRI17_OK;
+  }
   const int n = g.n[g.dim - 1];
   const int m = (n % 2 == 0) ? n / 2 : n;
   const int pitch = m + 1;
@@ -239,6 +271,14 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
 template <typename T, bool INV>
 static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
                         const Tables<T>& tab, BatchMask mask, cudaStream_t st) {
+  if (g.use_p8[1]) {
+    const Plan8& p = g.p8[1];
+    const int TB = (int)std::min<int64_t>(kP2Threads / p.T, g.H);
+    const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
+    dim3 grid((unsigned)((g.H + TB - 1) / TB), (unsigned)nouter);
+    axis_c2c_p2<T, INV><<<grid, p.T * TB, smem, st>>>(X, g.H, TB, p, tab.tw[1], mask);
+    return BRI17_OK;
+  }
   const int n = g.n[1];
   const int64_t B = g.H;
   const int pitch = n + 1;
@@ -258,6 +298,15 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
   constexpr int CIN = MODE == kModeRhs ? SYM : DIM;
   constexpr int COUT = MODE == kModeStrain ? SYM : DIM;
   constexpr int CMAX = CIN > COUT ? CIN : COUT;
+  if (MODE == kModeStiffness && g.use_p8[0]) {
+    const Plan8& p = g.p8[0];
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / p.T, g.P));
+    const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
+    dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
+    axis0_stiffness_p2<T, DIM><<<grid, p.T * TB, smem, st>>>(X, g.P, g.cspec, bstride, TB,
+                                                             p, fp, mask);
+    return BRI17_OK;
+  }
   const int n0 = g.n[0];
   const int pitch = n0 + 1;
   const size_t per_line = (size_t)(CMAX + 1) * pitch * sizeof(cplx<T>);
@@ -777,6 +826,7 @@ extern "C" int bri17_op_create(int dim, const int* shape, const double* L,
   g.cspec = (int64_t)g.n[0] * g.P;
   bool ok = make_plan(nl % 2 == 0 ? nl / 2 : nl, &g.plan_row);
   for (int i = 0; i < dim; i++) ok = ok && make_plan(g.n[i], &g.plan[i]);
+  set_p8_plans(&g);
   if (!ok) {
     delete op;
     set_error("axis length has a prime factor above 61");

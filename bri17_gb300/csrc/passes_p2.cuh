@@ -1,0 +1,201 @@
+// passes_p2.cuh -- the operator's FFT passes for power-of-two axis lengths,
+// on the register-resident engine of fft8.cuh.  Same data layout, same
+// results (to rounding) and same pass structure as passes.cuh, which keeps
+// serving every other length.
+#pragma once
+
+#include "fft8.cuh"
+#include "passes.cuh"
+
+namespace bri17gb {
+
+constexpr int kP2Threads = 256;
+constexpr int kP2FusedThreads = 128;
+
+// Last axis, forward (n = 2m, m a power of two >= 8): rows of n reals ->
+// n/2+1 complex.  T = m/8 threads per row, RB rows per CTA.
+template <typename T>
+__global__ void __launch_bounds__(kP2Threads)
+    rows_r2c_p2(const T* __restrict__ x, cplx<T>* __restrict__ X, int64_t nrows, int H,
+                Plan8 pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = pm.n, n = 2 * m, TT = pm.T;
+  const int pitch = pitch8(m);
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* bufs = tw + n;
+  const int64_t row0 = (int64_t)blockIdx.x * RB;
+  if (mask.skip(row0)) return;
+  const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
+  const int64_t row = row0 + rb;
+  const bool valid = rb < RB && row < nrows;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  cplx<T> v[8];
+  const cplx<T>* xc = reinterpret_cast<const cplx<T>*>(x) + row * m;
+#pragma unroll
+  for (int q = 0; q < 8; q++) v[q] = valid ? xc[t + TT * q] : mk<T>(T(0), T(0));
+  __syncthreads();
+  cplx<T>* buf = bufs + rb * pitch;
+  fft8_line<T, false>(v, buf, t, pm, tw, 2);
+#pragma unroll
+  for (int q = 0; q < 8; q++) buf[pad16(t + TT * q)] = v[q];
+  __syncthreads();
+  if (!valid) return;
+  cplx<T>* out = X + row * H;
+  const T h = T(0.5);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int k = t + TT * q;
+    const cplx<T> zk = v[q];
+    const cplx<T> zm = buf[pad16((m - k) & (m - 1))];
+    const cplx<T> e = mk<T>(h * (zk.x + zm.x), h * (zk.y - zm.y));
+    const cplx<T> o = mk<T>(h * (zk.y + zm.y), h * (zm.x - zk.x));
+    out[k] = cadd<T>(e, cmul<T>(tw[k], o));
+  }
+  if (t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
+}
+
+// Last axis, inverse: n/2+1 complex -> n reals (unnormalised).
+template <typename T>
+__global__ void __launch_bounds__(kP2Threads)
+    rows_c2r_p2(const cplx<T>* __restrict__ X, T* __restrict__ x, int64_t nrows, int H,
+                Plan8 pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = pm.n, n = 2 * m, TT = pm.T;
+  const int pitch = pitch8(m);
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* bufs = tw + n;
+  const int64_t row0 = (int64_t)blockIdx.x * RB;
+  if (mask.skip(row0)) return;
+  const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
+  const int64_t row = row0 + rb;
+  const bool valid = rb < RB && row < nrows;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  __syncthreads();
+  cplx<T> v[8];
+  const cplx<T>* in = X + row * H;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int k = t + TT * q;
+    if (valid) {
+      const cplx<T> xk = in[k];
+      const cplx<T> xm = in[m - k];
+      const cplx<T> A = mk<T>(xk.x + xm.x, xk.y - xm.y);
+      const cplx<T> D = mk<T>(xk.x - xm.x, xk.y + xm.y);
+      const cplx<T> Bv = cmulc<T>(D, tw[k]);
+      v[q] = mk<T>(A.x - Bv.y, A.y + Bv.x);
+    } else {
+      v[q] = mk<T>(T(0), T(0));
+    }
+  }
+  fft8_line<T, true>(v, bufs + rb * pitch, t, pm, tw, 2);
+  if (!valid) return;
+  cplx<T>* xc = reinterpret_cast<cplx<T>*>(x) + row * m;
+#pragma unroll
+  for (int q = 0; q < 8; q++) xc[t + TT * q] = v[q];
+}
+
+// Middle axis: complex [A][n][B], lines along n; TB consecutive inner
+// indices per CTA, consecutive threads on consecutive lines (coalesced).
+template <typename T, bool INV>
+__global__ void __launch_bounds__(kP2Threads)
+    axis_c2c_p2(cplx<T>* __restrict__ X, int64_t B, int TB, Plan8 p,
+                const cplx<T>* __restrict__ tw_g, BatchMask mask) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = p.n;
+  const int pitch = pitch8(n);
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* bufs = tw + n;
+  if (mask.skip(blockIdx.y)) return;
+  const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
+  const int64_t b = (int64_t)blockIdx.x * TB + tb;
+  const bool valid = b < B;
+  cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  cplx<T> v[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++)
+    v[q] = valid ? base[(int64_t)(t + p.T * q) * B] : mk<T>(T(0), T(0));
+  __syncthreads();
+  fft8_line<T, INV>(v, bufs + tb * pitch, t, p, tw, 1);
+  if (!valid) return;
+#pragma unroll
+  for (int q = 0; q < 8; q++) base[(int64_t)(t + p.T * q) * B] = v[q];
+}
+
+// Axis 0, fused stiffness: forward DFT of the DIM components along axis 0,
+// K(k) u(k) in registers, inverse DFT, in place (as axis0_fused with
+// kModeStiffness).
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kP2FusedThreads)
+    axis0_stiffness_p2(cplx<T>* __restrict__ X, int64_t P, int64_t cstride,
+                       int64_t bstride, int TB, Plan8 p0, FusedParams<T> fp,
+                       BatchMask mask) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n0 = p0.n;
+  const int pitch = pitch8(n0);
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* bufs = tw + n0;
+  if (mask.skip(blockIdx.y)) return;
+  const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
+  const int64_t b = (int64_t)blockIdx.x * TB + tb;
+  const bool valid = b < P;
+  cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
+  T s = fp.s, mu = fp.mu;
+  if (fp.mat) {
+    s = fp.mat[2 * blockIdx.y];
+    mu = fp.mat[2 * blockIdx.y + 1];
+  }
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  cplx<T>* buf = bufs + tb * pitch;
+  cplx<T> v[DIM][8];
+#pragma unroll
+  for (int c = 0; c < DIM; c++)
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      v[c][q] = valid ? base[c * cstride + (int64_t)(t + p0.T * q) * P]
+                      : mk<T>(T(0), T(0));
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < DIM; c++) fft8_line<T, false>(v[c], buf, t, p0, tw, 1);
+  int k1 = 0, k2 = 0;
+  if (valid) {
+    if constexpr (DIM == 3) {
+      k1 = (int)(b / fp.H);
+      k2 = (int)(b - (int64_t)k1 * fp.H);
+    } else {
+      k1 = (int)b;
+    }
+  }
+  const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
+          psi1 = __ldg(fp.tab.kpsi[1] + k1);
+  T phi2 = T(0), chi2 = T(0), psi2 = T(0);
+  if constexpr (DIM == 3) {
+    phi2 = __ldg(fp.tab.kphi[2] + k2);
+    chi2 = __ldg(fp.tab.kchi[2] + k2);
+    psi2 = __ldg(fp.tab.kpsi[2] + k2);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int k0 = t + p0.T * q;
+    const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
+            psi0 = __ldg(fp.tab.kpsi[0] + k0);
+    cplx<T> u[DIM];
+#pragma unroll
+    for (int c = 0; c < DIM; c++) u[c] = v[c][q];
+    if constexpr (DIM == 3)
+      stiffness3<T>(phi0, chi0, psi0, phi1, chi1, psi1, phi2, chi2, psi2, s, mu, u);
+    else
+      stiffness2<T>(phi0, chi0, psi0, phi1, chi1, psi1, s, mu, u);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) v[c][q] = u[c];
+  }
+#pragma unroll
+  for (int c = 0; c < DIM; c++) fft8_line<T, true>(v[c], buf, t, p0, tw, 1);
+  if (!valid) return;
+#pragma unroll
+  for (int c = 0; c < DIM; c++)
+#pragma unroll
+    for (int q = 0; q < 8; q++) base[c * cstride + (int64_t)(t + p0.T * q) * P] = v[c][q];
+}
+
+}  // namespace bri17gb
