@@ -22,6 +22,8 @@ struct bri17_op {
   void* stage_in;      // host-API staging buffers (lazy)
   void* stage_out;
   size_t stage_bytes;
+  cudaStream_t copy_stream;   // host-API copies (lazy)
+  cudaEvent_t host_events[7]; // host-API pipeline events (lazy)
 
   // Conjugate-gradient work space (lazy, owned by cg.cu).
   void* cg_work;

@@ -885,6 +885,10 @@ extern "C" int bri17_op_destroy(bri17_op* op) {
   cudaFree(op->spec);
   cudaFree(op->stage_in);
   cudaFree(op->stage_out);
+  if (op->copy_stream) {
+    cudaStreamDestroy(op->copy_stream);
+    for (int i = 0; i < 7; i++) cudaEventDestroy(op->host_events[i]);
+  }
   if (op->cg_work && op->cg_free) op->cg_free(op->cg_work);
   delete reinterpret_cast<PassTiming*>(op->timing);
   delete op;
@@ -959,6 +963,77 @@ extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
   return apply_stiffness_async(op, u, f, (cudaStream_t)stream);
 }
 
+// f = K u from host buffers, pipelined per component: the copy stream
+// uploads component c while the compute stream runs the forward passes of
+// component c-1, and downloads component c while the inverse passes of
+// component c+1 run.  Only the axis-0 pass needs all components at once.
+template <typename T>
+static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
+                                cudaStream_t st) {
+  const Geometry& g = op->g;
+  const int dim = g.dim;
+  const int64_t rows_per_comp = g.size / g.n[dim - 1];
+  const size_t cbytes = (size_t)g.size * sizeof(T);
+  const Tables<T>& tab = *reinterpret_cast<const Tables<T>*>(
+      op->precision == BRI17_F64 ? (const void*)&op->tab64 : (const void*)&op->tab32);
+  T* din = reinterpret_cast<T*>(op->stage_in);
+  T* dout = reinterpret_cast<T*>(op->stage_out);
+  cplx<T>* S = reinterpret_cast<cplx<T>*>(op->spec);
+  cudaEvent_t* ev = op->host_events;  // [0] start, [1..3] in, [4..6] out
+  BatchMask none;
+  none.flags = nullptr;
+  none.stride = 0;
+  none.unit = 1;
+  set_smem_attrs<T>();
+  cudaStream_t cp = op->copy_stream;
+  BRI17_CUDA_TRY(cudaEventRecord(ev[0], st));
+  BRI17_CUDA_TRY(cudaStreamWaitEvent(cp, ev[0], 0));
+  for (int c = 0; c < dim; c++) {
+    BRI17_CUDA_TRY(cudaMemcpyAsync(din + c * g.size, u_host + c * g.size, cbytes,
+                                   cudaMemcpyHostToDevice, cp));
+    BRI17_CUDA_TRY(cudaEventRecord(ev[1 + c], cp));
+  }
+  for (int c = 0; c < dim; c++) {
+    BRI17_CUDA_TRY(cudaStreamWaitEvent(st, ev[1 + c], 0));
+    {
+      PassScope ps(op, 0, st);
+      launch_rows_r2c<T>(g, din + c * g.size, S + c * g.cspec, rows_per_comp, tab, none, st);
+    }
+    if (dim == 3) {
+      PassScope ps(op, 1, st);
+      launch_axis1<T, false>(g, S + c * g.cspec, g.n[0], tab, none, st);
+    }
+  }
+  FusedParams<T> fp = fused_params<T>(op, tab, kModeStiffness);
+  int rc;
+  {
+    PassScope ps(op, 2, st);
+    if (dim == 3)
+      rc = launch_fused<T, 3, kModeStiffness>(g, S, 1, (int64_t)dim * g.cspec, fp, none, st);
+    else
+      rc = launch_fused<T, 2, kModeStiffness>(g, S, 1, (int64_t)dim * g.cspec, fp, none, st);
+  }
+  if (rc != BRI17_OK) return rc;
+  for (int c = 0; c < dim; c++) {
+    if (dim == 3) {
+      PassScope ps(op, 3, st);
+      launch_axis1<T, true>(g, S + c * g.cspec, g.n[0], tab, none, st);
+    }
+    {
+      PassScope ps(op, 4, st);
+      launch_rows_c2r<T>(g, S + c * g.cspec, dout + c * g.size, rows_per_comp, tab, none, st);
+    }
+    BRI17_CUDA_TRY(cudaEventRecord(ev[4 + c], st));
+    BRI17_CUDA_TRY(cudaStreamWaitEvent(cp, ev[4 + c], 0));
+    BRI17_CUDA_TRY(cudaMemcpyAsync(f_host + c * g.size, dout + c * g.size, cbytes,
+                                   cudaMemcpyDeviceToHost, cp));
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "operator launch");
+  BRI17_CUDA_TRY(cudaStreamSynchronize(cp));
+  return BRI17_OK;
+}
+
 extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
                                           void* f_host, void* stream) {
   if (!op) return invalid("null handle");
@@ -974,12 +1049,16 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
     BRI17_CUDA_TRY(cudaMalloc(&op->stage_out, bytes));
     op->stage_bytes = bytes;
   }
-  BRI17_CUDA_TRY(cudaMemcpyAsync(op->stage_in, u_host, bytes, cudaMemcpyHostToDevice, st));
-  int rc = apply_stiffness_async(op, op->stage_in, op->stage_out, st);
+  if (!op->copy_stream) {
+    BRI17_CUDA_TRY(cudaStreamCreateWithFlags(&op->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 7; i++)
+      BRI17_CUDA_TRY(cudaEventCreateWithFlags(&op->host_events[i], cudaEventDisableTiming));
+  }
+  int rc = ensure_spectrum(op, op->g.dim);
   if (rc != BRI17_OK) return rc;
-  BRI17_CUDA_TRY(cudaMemcpyAsync(f_host, op->stage_out, bytes, cudaMemcpyDeviceToHost, st));
-  BRI17_CUDA_TRY(cudaStreamSynchronize(st));
-  return BRI17_OK;
+  if (op->precision == BRI17_F64)
+    return apply_host_pipelined<double>(op, (const double*)u_host, (double*)f_host, st);
+  return apply_host_pipelined<float>(op, (const float*)u_host, (float*)f_host, st);
 }
 
 extern "C" int bri17_apply_strain(bri17_op* op, const void* u, void* eps,
