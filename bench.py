@@ -107,6 +107,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def aggregate_replicas(ms_local: float, units_per_step: int, steps: int, device=None):
+    """Whole-job throughput of independent replicas: every rank processed
+    `units_per_step * steps` units; the job time is the max over ranks.
+    Returns (value in G units/s, max ms).  Works on any torch.distributed
+    backend (a CPU tensor for gloo, a CUDA tensor for nccl)."""
+    import torch
+    import torch.distributed as dist
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t_max = ms_local
+    if ws > 1:
+        t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    return ws * units_per_step * steps / (t_max * 1e-3) / 1e9, t_max
+
+
 def make_u(shape, seed, dtype=np.float64):
     rng = np.random.default_rng(seed)
     u = rng.standard_normal((len(shape),) + tuple(shape))
@@ -300,12 +316,7 @@ def run_operator(args, precision="f64"):
     L.bri17_op_set_pass_timing(hooke.handle, 0)
     passes = {L.bri17_pass_name(i).decode(): {"ms_total": pms[i], "launches": pn[i]}
               for i in range(5) if pn[i] > 0}
-    t_max = ms_total
-    if ws > 1:
-        t = torch.tensor([ms_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = ws * dof * args.steps / (t_max * 1e-3) / 1e9
+    value, t_max = aggregate_replicas(ms_total, dof, args.steps, device="cuda")
     # Correctness of the timed output (first set) against a fresh apply.
     check = hooke.apply_stiffness(us[0])
     assert torch.equal(check, fs[0]) or args.steps == 0
