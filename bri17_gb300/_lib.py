@@ -28,7 +28,7 @@ STATUS = {
     8: "busy", 9: "not found", 10: "cancelled",
 }
 F64, F32 = 0, 1
-CG_PLAIN, CG_MIXED = 0, 1
+CG_PLAIN, CG_MIXED, CG_MIXED_RESTART = 0, 1, 2
 
 
 class CgInfo(ctypes.Structure):

@@ -269,7 +269,8 @@ class Hooke:
         rc = _lib.load().bri17_cg_solve(
             self._h, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr()),
             float(tol), int(max_iterations),
-            _lib.CG_MIXED if mode == "mixed" else _lib.CG_PLAIN, ctypes.byref(info),
+            {"plain": _lib.CG_PLAIN, "mixed": _lib.CG_MIXED,
+             "mixed_restart": _lib.CG_MIXED_RESTART}[mode], ctypes.byref(info),
             _stream_ptr(stream))
         out = {"iterations": info.iterations, "outer_iterations": info.outer_iterations,
                "rel_residual": info.rel_residual, "status": info.status,

@@ -191,6 +191,14 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
+// Reliable update: the recursive FP32 residual was just replaced by the
+// FP64 one (aux = its squared norm); keep the search direction, resume.
+__global__ void k_reliable_resume(CgState* st) {
+  st->rr = st->aux;
+  st->flag = BRI17_OK;
+  st->active = (st->aux > st->thresh && isfinite(st->aux)) ? 1 : 0;
+}
+
 // ---------------------------------------------------------------------------
 // Host side.
 
@@ -578,6 +586,142 @@ static int solve_mixed(bri17_op* op, const double* b, double* x, double tol,
   return status;
 }
 
+// Mixed precision with reliable updates (Clark et al., "Solving lattice
+// QCD systems of equations using mixed precision solvers on GPUs", 2010):
+// one FP32 CG whose search direction is kept throughout; whenever its
+// recursive residual has dropped by kDelta since the last update (or meets
+// the tolerance), the FP32 correction is folded into the FP64 iterate, the
+// residual is recomputed in FP64 (r = b - K x, zero-mean projection) and
+// replaces the FP32 one.  The solve stops on the FP64 residual.
+static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double tol,
+                                int maxit, bri17_cg_info* info) {
+  constexpr double kDelta = 0.1;
+  if (op->precision != BRI17_F64) {
+    set_error("mixed-precision CG needs an FP64 handle");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  if (!op->twin32) {
+    int shape[3] = {op->g.n[0], op->g.n[1], op->g.n[2]};
+    int rc = bri17_op_create(op->g.dim, shape, op->L, op->mu, op->nu, BRI17_F32,
+                             &op->twin32);
+    if (rc != BRI17_OK) return rc;
+  }
+  bri17_op* op32 = op->twin32;
+  CgWork* w;
+  int rc = ensure_work(op, true, &w);
+  if (rc != BRI17_OK) return rc;
+  const int64_t n = w->n;
+  cudaStream_t s = w->stream;
+  const int rb = red_blocks(n);
+  BRI17_CUDA_TRY(cudaMemcpyAsync(w->x, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  const double bb = w->st_host->aux;
+  info->iterations = 0;
+  info->outer_iterations = 0;
+  if (!isfinite(bb)) {
+    set_error("right-hand side is not finite");
+    return BRI17_ERR_BREAKDOWN;
+  }
+  if (!(bb > 0.0)) {
+    BRI17_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+    BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+    info->rel_residual = 0.0;
+    info->status = BRI17_OK;
+    return BRI17_OK;
+  }
+  // r = b - K x (FP64), projected; FP32 copies; p = r32; d = 0.
+  auto true_residual = [&](double* rr_out) -> int {
+    project_mean(op, w, w->x);
+    int e = residual64(op, w, b);
+    if (e != BRI17_OK) return e;
+    project_mean(op, w, w->r);
+    k_dot<double><<<rb, kRedThreads, 0, s>>>(w->r, w->r, n, w->st, w->partials);
+    e = read_state(w);
+    if (e != BRI17_OK) return e;
+    *rr_out = w->st_host->aux;
+    return BRI17_OK;
+  };
+  double rr64;
+  rc = true_residual(&rr64);
+  if (rc != BRI17_OK) return rc;
+  double rel = sqrt(rr64 / bb);
+  int status = BRI17_ERR_NOT_CONVERGED;
+  if (rel <= tol) status = BRI17_OK;
+  if (status != BRI17_OK) {
+    k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0, n);
+    BRI17_CUDA_TRY(cudaMemsetAsync(w->d32, 0, n * sizeof(float), s));
+    // aux = b.b so that k_start's threshold is tol^2 b.b.
+    k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
+    k_start<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->p32, n, w->st, w->partials,
+                                             tol * tol);
+    rc = get_graph<float>(op32, w, w->d32, w->r32, w->p32, w->q32, &w->graph32, &w->epoch32);
+    if (rc != BRI17_OK) return rc;
+    rc = read_state(w);
+    if (rc != BRI17_OK) return rc;
+    double rmax2 = rr64;  // squared norm at the last reliable update
+    int total = 0;
+    int breakdowns = 0;  // consecutive FP32 breakdowns (p.Kp <= 0 or NaN)
+    while (true) {
+      BRI17_CUDA_TRY(cudaGraphLaunch(w->graph32, s));
+      BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+      const CgState h = *w->st_host;
+      total = h.iters;
+      if (h.flag != BRI17_OK) {
+        // An FP32 breakdown is answered by a reliable update; two in a row
+        // without progress end the solve.
+        if (++breakdowns > 2) {
+          status = BRI17_ERR_BREAKDOWN;
+          break;
+        }
+      } else {
+        breakdowns = 0;
+      }
+      const bool dropped = h.rr < kDelta * kDelta * rmax2;
+      const bool budget = total >= maxit;
+      if (!(dropped || !h.active || budget)) continue;
+      // Reliable update: x += d (FP64), r = b - K x (FP64), r32 = r.
+      k_add_f32<<<grid1(n), 256, 0, s>>>(w->x, w->d32, 1.0, n);
+      BRI17_CUDA_TRY(cudaMemsetAsync(w->d32, 0, n * sizeof(float), s));
+      rc = true_residual(&rr64);
+      if (rc != BRI17_OK) return rc;
+      info->outer_iterations += 1;
+      if (!isfinite(rr64)) {
+        status = BRI17_ERR_BREAKDOWN;
+        break;
+      }
+      rel = sqrt(rr64 / bb);
+      if (rel <= tol) {
+        status = BRI17_OK;
+        break;
+      }
+      if (budget) {
+        status = BRI17_ERR_NOT_CONVERGED;
+        break;
+      }
+      rmax2 = rr64;
+      k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0, n);
+      k_dot<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->r32, n, w->st, w->partials);
+      k_reliable_resume<<<1, 1, 0, s>>>(w->st);
+      rc = read_state(w);
+      if (rc != BRI17_OK) return rc;
+      if (!w->st_host->active) {
+        // FP32 resolves no further: the recursive residual equals the
+        // replaced one and is already below the FP32 threshold.
+        status = BRI17_ERR_NOT_CONVERGED;
+        break;
+      }
+    }
+    info->iterations = total;
+  }
+  info->rel_residual = rel;
+  info->status = status;
+  BRI17_CUDA_TRY(cudaMemcpyAsync(x, w->x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  BRI17_CUDA_TRY(cudaStreamSynchronize(s));
+  return status;
+}
+
 }  // namespace bri17gb
 
 using namespace bri17gb;
@@ -592,14 +736,17 @@ extern "C" int bri17_cg_solve(bri17_op* op, const double* b, double* x,
     set_error("null pointer");
     return info->status = BRI17_ERR_INVALID_ARGUMENT;
   }
-  if (!(tol > 0) || max_iterations < 0 || (mode != BRI17_CG_PLAIN && mode != BRI17_CG_MIXED)) {
-    set_error("tol must be > 0, max_iterations >= 0, mode PLAIN or MIXED");
+  if (!(tol > 0) || max_iterations < 0 ||
+      (mode != BRI17_CG_PLAIN && mode != BRI17_CG_MIXED && mode != BRI17_CG_MIXED_RESTART)) {
+    set_error("tol must be > 0, max_iterations >= 0, mode PLAIN, MIXED or MIXED_RESTART");
     return info->status = BRI17_ERR_INVALID_ARGUMENT;
   }
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return info->status = cuda_fail(e, "cudaStreamSynchronize");
   int rc;
   if (mode == BRI17_CG_MIXED)
+    rc = solve_mixed_reliable(op, b, x, tol, max_iterations, info);
+  else if (mode == BRI17_CG_MIXED_RESTART)
     rc = solve_mixed(op, b, x, tol, max_iterations, info);
   else if (op->precision == BRI17_F64)
     rc = solve_plain64(op, b, x, tol, max_iterations, info);

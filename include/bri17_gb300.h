@@ -205,13 +205,19 @@ int bri17_eigenstress_rhs(bri17_op* op, const void* tau_dev, void* b_dev,
 
 /* Conjugate-gradient modes. */
 typedef enum bri17_cg_mode {
-  BRI17_CG_PLAIN = 0, /* CG in the handle's precision */
-  BRI17_CG_MIXED = 1  /* FP32 inner CG + FP64 residual/refinement outer loop */
+  BRI17_CG_PLAIN = 0,        /* CG in the handle's precision */
+  BRI17_CG_MIXED = 1,        /* FP32 CG with FP64 reliable updates: the FP32
+                                correction is folded into the FP64 iterate and
+                                the residual recomputed in FP64 (r = b - K x,
+                                zero-mean projection) each time it has dropped
+                                10x; the search direction is kept */
+  BRI17_CG_MIXED_RESTART = 2 /* classic iterative refinement: FP32 CG restarted
+                                on each FP64 residual */
 } bri17_cg_mode;
 
 typedef struct bri17_cg_info {
   int iterations;        /* total operator applications inside CG */
-  int outer_iterations;  /* refinement steps (mixed mode), else 1 */
+  int outer_iterations;  /* FP64 residual recomputations (mixed modes), else 1 */
   double rel_residual;   /* final ||b - K x|| / ||b|| (FP64, recomputed) */
   int status;            /* bri17_status of the solve */
 } bri17_cg_info;

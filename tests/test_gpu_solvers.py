@@ -30,7 +30,7 @@ def test_strain_matches_oracle(shape, L):
     assert rel_l2(eps, O.apply_strain(ho, u)) <= 1e-12
 
 
-@pytest.mark.parametrize("mode", ["plain", "mixed"])
+@pytest.mark.parametrize("mode", ["plain", "mixed", "mixed_restart"])
 @pytest.mark.parametrize("shape,nu", [((32, 32, 32), 0.3), ((24, 20, 16), 0.45), ((48, 40), 0.3)])
 def test_cg_matches_modal_direct_solve(mode, shape, nu):
     """CG to 1e-10 relative residual vs the exact FP64 per-mode solve;
