@@ -437,7 +437,7 @@ def run_cg(args, w, tau_fn, label):
     sols = {}
     sampler = ClockSampler(0)
     sampler.start()
-    for mode in ("mixed", "plain"):
+    for mode in ("mixed", "mixed_restart", "plain"):
         # warm-up: a short solve captures the graphs and builds the FP32 twin
         hooke.cg_solve(b, tol=1e-2, mode=mode, raise_on_failure=False)
         torch.cuda.synchronize()
@@ -469,7 +469,9 @@ def run_cg(args, w, tau_fn, label):
         "data": "synthetic",
         "config": {"workload": label, "grid": list(shape), "dof": dof, "tol": 1e-8,
                    "mu": w["mu"], "nu": w["nu"], "seed": w["seed"]},
-        "mixed": out["mixed"], "fp64": out["plain"],
+        "mixed": out["mixed"], "mixed_restart": out["mixed_restart"], "fp64": out["plain"],
+        "mixed_method": "FP32 CG with FP64 reliable updates (residual recomputed in FP64 "
+                        "each time it drops 10x; search direction kept)",
         "mixed_over_fp64_speedup": out["mixed"]["solves_per_s"] / out["plain"]["solves_per_s"],
         "error_vs_fp64_oracle": err, "clocks": clocks,
     }

@@ -18,6 +18,7 @@ struct CgState {
   double thresh;  // stop when rr <= thresh
   double aux;     // scratch result of helper reductions
   double mean[6]; // per-component means (projection)
+  double rmax2;   // reliable updates: squared FP64 residual at the last update
   int active;     // 1 while iterating
   int flag;       // BRI17_OK or BRI17_ERR_BREAKDOWN
   int iters;

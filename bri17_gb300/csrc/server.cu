@@ -15,9 +15,11 @@
 // Each bucket has its own stream; all buckets' graphs are launched before
 // any is waited on, so their work overlaps on the GPU.
 //
-// Per request (FP64 outer loop, as bri17_cg_solve's mixed mode): b = RHS(tau),
-// x = 0; repeat { r = b - K x (FP64), zero-mean projection, stop if
-// ||r|| <= tol ||b||; inner FP32 CG on K d = r / ||r||; x += ||r|| d }.
+// Per request (as bri17_cg_solve's mixed mode): b = RHS(tau), x = 0, one FP32
+// CG whose search direction is kept throughout; each time its recursive
+// residual has dropped 10x the slot pauses for an FP64 reliable update:
+// x += d, r = b - K x (FP64), zero-mean projection, stop if ||r|| <= tol
+// ||b||, else the FP32 residual is replaced by r and the slot resumes.
 // Admission is by device footprint: a new bucket is created only while the
 // server's total allocation stays within its memory budget.
 #include <math.h>
@@ -36,6 +38,7 @@ namespace bri17gb {
 namespace {
 
 constexpr int kSrvChunk = 16;  // inner iterations per graph replay
+constexpr double kDelta2 = 0.01;  // reliable update when |r32|^2 < kDelta2 |r64|^2
 
 struct Request {
   int64_t id;
@@ -47,7 +50,7 @@ struct Request {
   double tol;
   int max_iterations;
   double t_submit = 0, t_admit = 0, t_finish = 0;
-  int iters = 0, outer = 0;
+  int iters = 0, outer = 0, breakdowns = 0;
   double bb = 0, rel = 1, nr = 0;
   int status = BRI17_OK;
   bool cancel = false;
@@ -161,7 +164,10 @@ __global__ void __launch_bounds__(kRedThreads)
     }
     st->beta = tot / st->rr;
     st->rr = tot;
-    if (tot <= st->thresh || st->iters >= max_iters) st->active = 0;
+    // Pause for an FP64 reliable update once the FP32 residual has dropped
+    // by kDelta since the last one (or meets the tolerance).
+    if (tot <= st->thresh || st->iters >= max_iters || tot < kDelta2 * st->rmax2)
+      st->active = 0;
   }
 }
 
@@ -238,15 +244,15 @@ __global__ void ks_sub_mean(double* __restrict__ a, int64_t size, const CgState*
     ac[i] -= m;
 }
 
-// Inner CG restart: r32 = r * scale, d = 0, p = r32, rr, thresh, active.
+// FP32 CG start: r32 = r, p = r32, d = 0, rr, thresh (tol^2 b.b), rmax2.
 __global__ void __launch_bounds__(kRedThreads)
-    ks_restart(const double* __restrict__ r, double scale, float* __restrict__ r32,
-               float* __restrict__ d, float* __restrict__ p, int64_t n, CgState* st,
-               double* partials, double tin2) {
+    ks_start(const double* __restrict__ r, float* __restrict__ r32, float* __restrict__ d,
+             float* __restrict__ p, int64_t n, CgState* st, double* partials, double thresh,
+             double rmax2) {
   double v = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const float ri = (float)(r[i] * scale);
+    const float ri = (float)r[i];
     r32[i] = ri;
     p[i] = ri;
     d[i] = 0.f;
@@ -257,8 +263,33 @@ __global__ void __launch_bounds__(kRedThreads)
   slot_block_total(v, partials, &st->counter, gridDim.x, &tot, &last);
   if (last && threadIdx.x == 0) {
     st->rr = tot;
-    st->thresh = tin2 * tot;
+    st->thresh = thresh;
+    st->rmax2 = rmax2;
     st->iters = 0;
+    st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
+    st->active = (tot > thresh && isfinite(tot)) ? 1 : 0;
+  }
+}
+
+// Reliable update: the FP32 residual is replaced by the FP64 one, the
+// correction restarts from zero, the search direction p is kept.
+__global__ void __launch_bounds__(kRedThreads)
+    ks_reliable(const double* __restrict__ r, float* __restrict__ r32, float* __restrict__ d,
+                int64_t n, CgState* st, double* partials, double rmax2) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float ri = (float)r[i];
+    r32[i] = ri;
+    d[i] = 0.f;
+    v += (double)ri * (double)ri;
+  }
+  double tot;
+  bool last;
+  slot_block_total(v, partials, &st->counter, gridDim.x, &tot, &last);
+  if (last && threadIdx.x == 0) {
+    st->rr = tot;
+    st->rmax2 = rmax2;
     st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
     st->active = (tot > st->thresh && isfinite(tot)) ? 1 : 0;
   }
@@ -540,15 +571,17 @@ int outer_decide(bri17_server* srv, Bucket* B, int z, bool* busy) {
                              : converged ? BRI17_OK : BRI17_ERR_NOT_CONVERGED);
     return BRI17_OK;
   }
-  double tin = 0.1 * q->tol / q->rel;
-  if (tin < 1e-5) tin = 1e-5;
-  if (tin > 1e-2) tin = 1e-2;
-  q->nr = sqrt(rr);
-  q->outer += 1;
   const int64_t n = B->n;
-  ks_restart<<<red_blocks(n), kRedThreads, 0, B->stream>>>(
-      B->r + z * n, 1.0 / q->nr, B->r32 + z * n, B->d + z * n, B->p32 + z * n, n, B->st + z,
-      B->partials + z * kRedMaxBlocks, tin * tin);
+  if (q->outer == 0) {
+    ks_start<<<red_blocks(n), kRedThreads, 0, B->stream>>>(
+        B->r + z * n, B->r32 + z * n, B->d + z * n, B->p32 + z * n, n, B->st + z,
+        B->partials + z * kRedMaxBlocks, q->tol * q->tol * q->bb, rr);
+  } else {
+    ks_reliable<<<red_blocks(n), kRedThreads, 0, B->stream>>>(
+        B->r + z * n, B->r32 + z * n, B->d + z * n, n, B->st + z,
+        B->partials + z * kRedMaxBlocks, rr);
+  }
+  q->outer += 1;
   *busy = true;
   return BRI17_OK;
 }
@@ -718,20 +751,21 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
         ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
       }
       if (!h.active || q->cancel) {
-        q->iters += h.iters;
-        if (h.flag != BRI17_OK && h.iters == 0) {
+        q->iters = h.iters;  // cumulative: reliable updates keep the count
+        q->breakdowns = h.flag != BRI17_OK ? q->breakdowns + 1 : 0;
+        if (q->breakdowns > 2) {
           q->rel = NAN;
           B->slot_state[z] = kFree;
           B->slot_req[z] = nullptr;
           finish(srv, q, BRI17_ERR_BREAKDOWN);
           continue;
         }
-        ks_axpy32<<<g1(B->n), 256, 0, B->stream>>>(B->x + z * B->n, B->d + z * B->n, q->nr,
+        ks_axpy32<<<g1(B->n), 256, 0, B->stream>>>(B->x + z * B->n, B->d + z * B->n, 1.0,
                                                    B->n);
         int rc = enqueue_residual(B, z, false);
         if (rc != BRI17_OK) return rc;
         outer.push_back(z);
-      } else if (q->iters + h.iters >= q->max_iterations) {
+      } else if (h.iters >= q->max_iterations) {
         ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
       }
     }
