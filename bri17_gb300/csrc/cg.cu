@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kRedThreads)
     }
     st->beta = tot / st->rr;
     st->rr = tot;
-    if (tot <= st->thresh) st->active = 0;
+    if (tot <= st->thresh) st->pause = 1;
   }
 }
 
@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(kRedThreads)
     st->rr = tot;
     st->thresh = rel_tol2 * st->aux;
     st->iters = 0;
+    st->pause = 0;
     st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
     st->active = (tot > st->thresh && isfinite(tot)) ? 1 : 0;
   }
@@ -193,10 +194,13 @@ __global__ void __launch_bounds__(kRedThreads)
 
 // Reliable update: the recursive FP32 residual was just replaced by the
 // FP64 one (aux = its squared norm); keep the search direction, resume.
+// At least one more chunk runs even when the replaced residual already meets
+// the FP32 threshold, so every update changes the iterate.
 __global__ void k_reliable_resume(CgState* st) {
   st->rr = st->aux;
   st->flag = BRI17_OK;
-  st->active = (st->aux > st->thresh && isfinite(st->aux)) ? 1 : 0;
+  st->pause = 0;
+  st->active = isfinite(st->aux) ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -304,6 +308,7 @@ static int enqueue_chunk(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
     k_dot_pq<T><<<rb, kRedThreads, 0, s>>>(p, q, n, w->st, w->partials);
     k_update<T><<<rb, kRedThreads, 0, s>>>(x, r, p, q, n, w->st, w->partials);
     k_pupdate<T><<<grid1(n), 256, 0, s>>>(p, r, n, w->st);
+    k_apply_pause<<<1, 32, 0, s>>>(w->st, 1);
   }
   BRI17_CUDA_TRY(cudaMemcpyAsync(w->st_host, w->st, sizeof(CgState),
                                  cudaMemcpyDeviceToHost, s));
@@ -707,9 +712,7 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
       rc = read_state(w);
       if (rc != BRI17_OK) return rc;
       if (!w->st_host->active) {
-        // FP32 resolves no further: the recursive residual equals the
-        // replaced one and is already below the FP32 threshold.
-        status = BRI17_ERR_NOT_CONVERGED;
+        status = BRI17_ERR_BREAKDOWN;
         break;
       }
     }

@@ -183,12 +183,13 @@ static void set_smem_attrs() {
     cudaFuncSetAttribute(rows_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(axis_c2c<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(axis_c2c<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    cudaFuncSetAttribute(rows_r2c_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    cudaFuncSetAttribute(rows_c2r_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    cudaFuncSetAttribute(axis_c2c_p2<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    cudaFuncSetAttribute(axis_c2c_p2<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    cudaFuncSetAttribute(axis0_stiffness_p2<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    cudaFuncSetAttribute(axis0_stiffness_p2<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(rows_r2c_p2<T, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(rows_c2r_p2<T, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis_c2c_p2<T, false, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis_c2c_p2<T, true, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis0_stiffness_p2<T, 2, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    cudaFuncSetAttribute(axis0_stiffness_p2<T, 3, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    ct_set_smem_attrs(kMaxSmem);
 #define SET_FUSED(D, M) \
   cudaFuncSetAttribute(axis0_fused<T, D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem)
     SET_FUSED(2, kModeStiffness);
@@ -230,8 +231,9 @@ static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
     const Plan8& p = g.p8_row;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
     const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
-    rows_r2c_p2<T><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
-        x, X, nrows, g.H, p, tab.tw[g.dim - 1], rb, mask);
+    if (!ct_rows_r2c<T>(p.n, x, X, nrows, g.H, tab.tw[g.dim - 1], rb, smem, mask, st))
+      rows_r2c_p2<T, RtEng><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
+          x, X, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
     return BRI17_OK;
   }
   const int n = g.n[g.dim - 1];
@@ -253,8 +255,9 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
     const Plan8& p = g.p8_row;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
     const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
-    rows_c2r_p2<T><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
-        X, x, nrows, g.H, p, tab.tw[g.dim - 1], rb, mask);
+    if (!ct_rows_c2r<T>(p.n, X, x, nrows, g.H, tab.tw[g.dim - 1], rb, smem, mask, st))
+      rows_c2r_p2<T, RtEng><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
+          X, x, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
     return BRI17_OK;
   }
   const int n = g.n[g.dim - 1];
@@ -276,7 +279,9 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
     const int TB = (int)std::min<int64_t>(kP2Threads / p.T, g.H);
     const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.H + TB - 1) / TB), (unsigned)nouter);
-    axis_c2c_p2<T, INV><<<grid, p.T * TB, smem, st>>>(X, g.H, TB, p, tab.tw[1], mask);
+    if (!ct_axis_c2c<T, INV>(p.n, X, g.H, TB, grid, smem, tab.tw[1], mask, st))
+      axis_c2c_p2<T, INV, RtEng><<<grid, p.T * TB, smem, st>>>(X, g.H, TB, RtEng{p}, tab.tw[1],
+                                                               mask);
     return BRI17_OK;
   }
   const int n = g.n[1];
@@ -303,8 +308,10 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / p.T, g.P));
     const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
-    axis0_stiffness_p2<T, DIM><<<grid, p.T * TB, smem, st>>>(X, g.P, g.cspec, bstride, TB,
-                                                             p, fp, mask);
+    if (!ct_axis0_stiffness<T, DIM>(p.n, X, g.P, g.cspec, bstride, TB, grid, smem, fp, mask,
+                                    st))
+      axis0_stiffness_p2<T, DIM, RtEng><<<grid, p.T * TB, smem, st>>>(
+          X, g.P, g.cspec, bstride, TB, RtEng{p}, fp, mask);
     return BRI17_OK;
   }
   const int n0 = g.n[0];

@@ -5,21 +5,46 @@
 #pragma once
 
 #include "fft8.cuh"
+#include "fft8_ct.cuh"
 #include "passes.cuh"
 
 namespace bri17gb {
+
+// Engine policies: the kernels below take either the runtime-plan engine
+// (any power-of-two length) or a compile-time-length engine.
+struct RtEng {
+  Plan8 p;
+  __device__ __forceinline__ int n() const { return p.n; }
+  __device__ __forceinline__ int T() const { return p.T; }
+  template <typename S, bool INV>
+  __device__ __forceinline__ void run(cplx<S> (&v)[8], cplx<S>* buf, int t,
+                                      const cplx<S>* __restrict__ tw, int tws) const {
+    fft8_line<S, INV>(v, buf, t, p, tw, tws);
+  }
+};
+
+template <int N>
+struct CtEng {
+  __device__ __forceinline__ constexpr int n() const { return N; }
+  __device__ __forceinline__ constexpr int T() const { return N / 8; }
+  template <typename S, bool INV>
+  __device__ __forceinline__ void run(cplx<S> (&v)[8], cplx<S>* buf, int t,
+                                      const cplx<S>* __restrict__ tw, int tws) const {
+    fft8_ct<S, N, INV>(v, buf, t, tw, tws);
+  }
+};
 
 constexpr int kP2Threads = 256;
 constexpr int kP2FusedThreads = 128;
 
 // Last axis, forward (n = 2m, m a power of two >= 8): rows of n reals ->
 // n/2+1 complex.  T = m/8 threads per row, RB rows per CTA.
-template <typename T>
+template <typename T, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     rows_r2c_p2(const T* __restrict__ x, cplx<T>* __restrict__ X, int64_t nrows, int H,
-                Plan8 pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
+                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int m = pm.n, n = 2 * m, TT = pm.T;
+  const int m = pm.n(), n = 2 * m, TT = pm.T();
   const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
@@ -35,7 +60,7 @@ __global__ void __launch_bounds__(kP2Threads)
   for (int q = 0; q < 8; q++) v[q] = valid ? xc[t + TT * q] : mk<T>(T(0), T(0));
   __syncthreads();
   cplx<T>* buf = bufs + rb * pitch;
-  fft8_line<T, false>(v, buf, t, pm, tw, 2);
+  pm.template run<T, false>(v, buf, t, tw, 2);
 #pragma unroll
   for (int q = 0; q < 8; q++) buf[pad16(t + TT * q)] = v[q];
   __syncthreads();
@@ -55,12 +80,12 @@ __global__ void __launch_bounds__(kP2Threads)
 }
 
 // Last axis, inverse: n/2+1 complex -> n reals (unnormalised).
-template <typename T>
+template <typename T, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     rows_c2r_p2(const cplx<T>* __restrict__ X, T* __restrict__ x, int64_t nrows, int H,
-                Plan8 pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
+                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int m = pm.n, n = 2 * m, TT = pm.T;
+  const int m = pm.n(), n = 2 * m, TT = pm.T();
   const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
@@ -87,7 +112,7 @@ __global__ void __launch_bounds__(kP2Threads)
       v[q] = mk<T>(T(0), T(0));
     }
   }
-  fft8_line<T, true>(v, bufs + rb * pitch, t, pm, tw, 2);
+  pm.template run<T, true>(v, bufs + rb * pitch, t, tw, 2);
   if (!valid) return;
   cplx<T>* xc = reinterpret_cast<cplx<T>*>(x) + row * m;
 #pragma unroll
@@ -96,12 +121,12 @@ __global__ void __launch_bounds__(kP2Threads)
 
 // Middle axis: complex [A][n][B], lines along n; TB consecutive inner
 // indices per CTA, consecutive threads on consecutive lines (coalesced).
-template <typename T, bool INV>
+template <typename T, bool INV, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
-    axis_c2c_p2(cplx<T>* __restrict__ X, int64_t B, int TB, Plan8 p,
+    axis_c2c_p2(cplx<T>* __restrict__ X, int64_t B, int TB, Eng p,
                 const cplx<T>* __restrict__ tw_g, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n = p.n;
+  const int n = p.n();
   const int pitch = pitch8(n);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
@@ -114,24 +139,24 @@ __global__ void __launch_bounds__(kP2Threads)
   cplx<T> v[8];
 #pragma unroll
   for (int q = 0; q < 8; q++)
-    v[q] = valid ? base[(int64_t)(t + p.T * q) * B] : mk<T>(T(0), T(0));
+    v[q] = valid ? base[(int64_t)(t + p.T() * q) * B] : mk<T>(T(0), T(0));
   __syncthreads();
-  fft8_line<T, INV>(v, bufs + tb * pitch, t, p, tw, 1);
+  p.template run<T, INV>(v, bufs + tb * pitch, t, tw, 1);
   if (!valid) return;
 #pragma unroll
-  for (int q = 0; q < 8; q++) base[(int64_t)(t + p.T * q) * B] = v[q];
+  for (int q = 0; q < 8; q++) base[(int64_t)(t + p.T() * q) * B] = v[q];
 }
 
 // Axis 0, fused stiffness: forward DFT of the DIM components along axis 0,
 // K(k) u(k) in registers, inverse DFT, in place (as axis0_fused with
 // kModeStiffness).
-template <typename T, int DIM>
+template <typename T, int DIM, class Eng>
 __global__ void __launch_bounds__(kP2FusedThreads)
     axis0_stiffness_p2(cplx<T>* __restrict__ X, int64_t P, int64_t cstride,
-                       int64_t bstride, int TB, Plan8 p0, FusedParams<T> fp,
+                       int64_t bstride, int TB, Eng p0, FusedParams<T> fp,
                        BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n0 = p0.n;
+  const int n0 = p0.n();
   const int pitch = pitch8(n0);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n0;
@@ -152,11 +177,11 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   for (int c = 0; c < DIM; c++)
 #pragma unroll
     for (int q = 0; q < 8; q++)
-      v[c][q] = valid ? base[c * cstride + (int64_t)(t + p0.T * q) * P]
+      v[c][q] = valid ? base[c * cstride + (int64_t)(t + p0.T() * q) * P]
                       : mk<T>(T(0), T(0));
   __syncthreads();
 #pragma unroll
-  for (int c = 0; c < DIM; c++) fft8_line<T, false>(v[c], buf, t, p0, tw, 1);
+  for (int c = 0; c < DIM; c++) p0.template run<T, false>(v[c], buf, t, tw, 1);
   int k1 = 0, k2 = 0;
   if (valid) {
     if constexpr (DIM == 3) {
@@ -176,7 +201,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   }
 #pragma unroll
   for (int q = 0; q < 8; q++) {
-    const int k0 = t + p0.T * q;
+    const int k0 = t + p0.T() * q;
     const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
             psi0 = __ldg(fp.tab.kpsi[0] + k0);
     cplx<T> u[DIM];
@@ -190,12 +215,34 @@ __global__ void __launch_bounds__(kP2FusedThreads)
     for (int c = 0; c < DIM; c++) v[c][q] = u[c];
   }
 #pragma unroll
-  for (int c = 0; c < DIM; c++) fft8_line<T, true>(v[c], buf, t, p0, tw, 1);
+  for (int c = 0; c < DIM; c++) p0.template run<T, true>(v[c], buf, t, tw, 1);
   if (!valid) return;
 #pragma unroll
   for (int c = 0; c < DIM; c++)
 #pragma unroll
-    for (int q = 0; q < 8; q++) base[c * cstride + (int64_t)(t + p0.T * q) * P] = v[c][q];
+    for (int q = 0; q < 8; q++) base[c * cstride + (int64_t)(t + p0.T() * q) * P] = v[c][q];
 }
+
+}  // namespace bri17gb
+
+namespace bri17gb {
+
+// Launchers of the compile-time-length kernels (passes_ct.cuh, instantiated
+// in passes_ct_f32.cu / passes_ct_f64.cu).  Each returns false, launching
+// nothing, when the length has no compile-time instance.
+template <typename T>
+bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx<T>* tw,
+                 int RB, size_t smem, BatchMask mask, cudaStream_t st);
+template <typename T>
+bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx<T>* tw,
+                 int RB, size_t smem, BatchMask mask, cudaStream_t st);
+template <typename T, bool INV>
+bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int TB, dim3 grid, size_t smem,
+                 const cplx<T>* tw, BatchMask mask, cudaStream_t st);
+template <typename T, int DIM>
+bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t bstride,
+                        int TB, dim3 grid, size_t smem, const FusedParams<T>& fp,
+                        BatchMask mask, cudaStream_t st);
+void ct_set_smem_attrs(size_t max_smem);
 
 }  // namespace bri17gb

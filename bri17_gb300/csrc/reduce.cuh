@@ -20,11 +20,11 @@ struct CgState {
   double mean[6]; // per-component means (projection)
   double rmax2;   // reliable updates: squared FP64 residual at the last update
   int active;     // 1 while iterating
+  int pause;      // set by the update kernel: stop after this iteration's
+                  // search-direction update (k_apply_pause)
   int flag;       // BRI17_OK or BRI17_ERR_BREAKDOWN
   int iters;
-  int pad;
   unsigned int counter;  // last-block ticket
-  unsigned int pad2;
 };
 
 inline int red_blocks(int64_t n) {
@@ -76,5 +76,15 @@ __device__ __forceinline__ bool last_block_total(double v, double* partials,
   return true;
 }
 
+
+// Ends iteration for states whose update kernel asked to pause: runs after
+// the search-direction update, so a paused CG resumes with a consistent p.
+static __global__ void k_apply_pause(CgState* sts, int count) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z < count && sts[z].pause) {
+    sts[z].active = 0;
+    sts[z].pause = 0;
+  }
+}
 
 }  // namespace bri17gb

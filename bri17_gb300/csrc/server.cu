@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kRedThreads)
     // Pause for an FP64 reliable update once the FP32 residual has dropped
     // by kDelta since the last one (or meets the tolerance).
     if (tot <= st->thresh || st->iters >= max_iters || tot < kDelta2 * st->rmax2)
-      st->active = 0;
+      st->pause = 1;
   }
 }
 
@@ -266,6 +266,7 @@ __global__ void __launch_bounds__(kRedThreads)
     st->thresh = thresh;
     st->rmax2 = rmax2;
     st->iters = 0;
+    st->pause = 0;
     st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
     st->active = (tot > thresh && isfinite(tot)) ? 1 : 0;
   }
@@ -290,8 +291,10 @@ __global__ void __launch_bounds__(kRedThreads)
   if (last && threadIdx.x == 0) {
     st->rr = tot;
     st->rmax2 = rmax2;
+    st->pause = 0;
     st->flag = isfinite(tot) ? BRI17_OK : BRI17_ERR_BREAKDOWN;
-    st->active = (tot > st->thresh && isfinite(tot)) ? 1 : 0;
+    // At least one more chunk runs, so every update changes the iterate.
+    st->active = isfinite(tot) ? 1 : 0;
   }
 }
 
@@ -382,6 +385,7 @@ int capture_graph(Bucket* B) {
                                            B->partials, 1 << 30);
     dim3 g2(g1(n), B->S);
     kb_pupdate<<<g2, 256, 0, s>>>(B->p32, B->r32, n, B->st);
+    k_apply_pause<<<1, 64, 0, s>>>(B->st, B->S);
   }
   cudaMemcpyAsync(B->st_host, B->st, B->S * sizeof(CgState), cudaMemcpyDeviceToHost, s);
   cudaError_t e = cudaStreamEndCapture(s, &g);

@@ -80,3 +80,20 @@ def test_cg_warm_start_and_material_change():
     ho2 = O.Hooke(2.0, 0.2, ho.grid)
     x3, info3 = h.cg_solve(b, tol=1e-10, mode="mixed")
     assert rel_l2(x3.cpu().numpy(), O.eigenstress_solve(ho2, tau)) <= 1e-6
+
+
+@pytest.mark.parametrize("shape,nu", [((32, 32, 32), 0.3), ((48, 40), 0.45)])
+def test_mixed_reliable_keeps_fp64_iteration_count(shape, nu):
+    """Reliable updates keep the Krylov space: the mixed solve needs about as
+    many operator applications as plain FP64 CG (a solve that resumed with
+    a stale search direction after an update would need far more)."""
+    L = (1.0,) * len(shape)
+    h, _ = pair(shape, L, 1.0, nu)
+    sym = 3 if len(shape) == 2 else 6
+    tau = np.random.default_rng(12).standard_normal((sym,) + shape)
+    b = h.eigenstress_rhs(to_dev(tau))
+    _, plain = h.cg_solve(b, tol=1e-10, mode="plain")
+    _, mixed = h.cg_solve(b, tol=1e-10, mode="mixed")
+    assert mixed["status"] == 0 and plain["status"] == 0
+    assert mixed["iterations"] <= 1.3 * plain["iterations"] + 16, (mixed, plain)
+    assert mixed["outer_iterations"] >= 2
