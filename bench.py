@@ -336,6 +336,19 @@ def run_operator(args, precision="f64"):
     e2e_s = time.perf_counter() - t0
     e2e = {"value": dof * args.steps / e2e_s / 1e9, "unit": "GDoF/s",
            "h2d_bytes_per_step": dof * scalar, "d2h_bytes_per_step": dof * scalar}
+    # Breakdown: the copies alone (same pinned buffers, one stream).
+    dev = torch.empty_like(us[0])
+    c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    for _ in range(3):
+        c0.record()
+        dev.copy_(u_host, non_blocking=True)
+        c1.record()
+        f_host.copy_(dev, non_blocking=True)
+        c2.record()
+        c2.synchronize()
+    e2e["breakdown_ms"] = {"step": 1e3 * e2e_s / max(1, args.steps),
+                           "h2d_alone": c0.elapsed_time(c1), "d2h_alone": c1.elapsed_time(c2),
+                           "apply_device": t_max / max(1, args.steps)}
 
     hbm_peak, peak_kind = peaks()
     cspec = shape[0] * shape[1] * (shape[2] // 2 + 1)

@@ -230,7 +230,7 @@ static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
   if (g.use_p8_row) {
     const Plan8& p = g.p8_row;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
-    const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
+    const size_t smem = (3 * p.n + 1 + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
     if (!ct_rows_r2c<T>(p.n, x, X, nrows, g.H, tab.tw[g.dim - 1], rb, smem, mask, st))
       rows_r2c_p2<T, RtEng><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
           x, X, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);

@@ -47,13 +47,18 @@ __global__ void __launch_bounds__(kP2Threads)
   const int m = pm.n(), n = 2 * m, TT = pm.T();
   const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bufs = tw + n;
+  cplx<T>* twh = tw + n;        // W_n^k / 2, k in [0, m]
+  cplx<T>* bufs = twh + m + 1;
   const int64_t row0 = (int64_t)blockIdx.x * RB;
   if (mask.skip(row0)) return;
   const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const cplx<T> w = tw_g[i];
+    tw[i] = w;
+    if (i <= m) twh[i] = mk<T>(T(0.5) * w.x, T(0.5) * w.y);
+  }
   cplx<T> v[8];
   const cplx<T>* xc = reinterpret_cast<const cplx<T>*>(x) + row * m;
 #pragma unroll
@@ -66,15 +71,18 @@ __global__ void __launch_bounds__(kP2Threads)
   __syncthreads();
   if (!valid) return;
   cplx<T>* out = X + row * H;
-  const T h = T(0.5);
+  // X_k = (A + W D) / 2 with A = Z_k + conj(Z_{m-k}), D = -i (Z_k -
+  // conj(Z_{m-k})); the 1/2 lives in the twh table and one fused
+  // multiply-add per part.
 #pragma unroll
   for (int q = 0; q < 8; q++) {
     const int k = t + TT * q;
     const cplx<T> zk = v[q];
     const cplx<T> zm = buf[pad16((m - k) & (m - 1))];
-    const cplx<T> e = mk<T>(h * (zk.x + zm.x), h * (zk.y - zm.y));
-    const cplx<T> o = mk<T>(h * (zk.y + zm.y), h * (zm.x - zk.x));
-    out[k] = cadd<T>(e, cmul<T>(tw[k], o));
+    const cplx<T> A = mk<T>(zk.x + zm.x, zk.y - zm.y);
+    const cplx<T> D = mk<T>(zk.y + zm.y, zm.x - zk.x);
+    const cplx<T> WD = cmul<T>(twh[k], D);
+    out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
   }
   if (t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
 }
@@ -147,6 +155,67 @@ __global__ void __launch_bounds__(kP2Threads)
   for (int q = 0; q < 8; q++) base[(int64_t)(t + p.T() * q) * B] = v[q];
 }
 
+// Products of one spectrum line's axis-1/axis-2 factors of
+// Hooke::modal_stiffness (include/bri17/bri17.hpp:276-288): with them a
+// mode's K(k) costs one product per entry of H and per off-diagonal entry.
+template <typename T>
+struct LineFactors {
+  T c12;   // chi1 chi2      (H00 = phi0 c12)
+  T a1;    // phi1 chi2      (H11 = chi0 a1)
+  T a2;    // chi1 phi2      (H22 = chi0 a2)
+  T pc;    // psi1 chi2      (K01 = s psi0 pc)
+  T cp;    // chi1 psi2      (K02 = s psi0 cp)
+  T pp;    // psi1 psi2      (K12 = s chi0 pp)
+};
+
+template <typename T, int DIM>
+__device__ __forceinline__ LineFactors<T> line_factors(T phi1, T chi1, T psi1, T phi2, T chi2,
+                                                      T psi2) {
+  LineFactors<T> f;
+  if constexpr (DIM == 3) {
+    f.c12 = chi1 * chi2;
+    f.a1 = phi1 * chi2;
+    f.a2 = chi1 * phi2;
+    f.pc = psi1 * chi2;
+    f.cp = chi1 * psi2;
+    f.pp = psi1 * psi2;
+  } else {
+    f.c12 = chi1;
+    f.a1 = phi1;
+    f.a2 = T(0);
+    f.pc = psi1;
+    f.cp = T(0);
+    f.pp = T(0);
+  }
+  return f;
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ void stiffness_lf(T phi0, T chi0, T psi0, const LineFactors<T>& f,
+                                             T s, T mu, cplx<T>* u) {
+  const T H00 = phi0 * f.c12;
+  const T H11 = chi0 * f.a1;
+  const T sp0 = s * psi0;
+  const T K01 = sp0 * f.pc;
+  if constexpr (DIM == 3) {
+    const T H22 = chi0 * f.a2;
+    const T Kd = mu * (H00 + H11 + H22);
+    const T K00 = s * H00 + Kd, K11 = s * H11 + Kd, K22 = s * H22 + Kd;
+    const T K02 = sp0 * f.cp;
+    const T K12 = (s * chi0) * f.pp;
+    const cplx<T> u0 = u[0], u1 = u[1], u2 = u[2];
+    u[0] = mk<T>(K00 * u0.x + K01 * u1.x + K02 * u2.x, K00 * u0.y + K01 * u1.y + K02 * u2.y);
+    u[1] = mk<T>(K01 * u0.x + K11 * u1.x + K12 * u2.x, K01 * u0.y + K11 * u1.y + K12 * u2.y);
+    u[2] = mk<T>(K02 * u0.x + K12 * u1.x + K22 * u2.x, K02 * u0.y + K12 * u1.y + K22 * u2.y);
+  } else {
+    const T Kd = mu * (H00 + H11);
+    const T K00 = s * H00 + Kd, K11 = s * H11 + Kd;
+    const cplx<T> u0 = u[0], u1 = u[1];
+    u[0] = mk<T>(K00 * u0.x + K01 * u1.x, K00 * u0.y + K01 * u1.y);
+    u[1] = mk<T>(K01 * u0.x + K11 * u1.x, K01 * u0.y + K11 * u1.y);
+  }
+}
+
 // Axis 0, fused stiffness: forward DFT of the DIM components along axis 0,
 // K(k) u(k) in registers, inverse DFT, in place (as axis0_fused with
 // kModeStiffness).
@@ -193,12 +262,14 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   }
   const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
           psi1 = __ldg(fp.tab.kpsi[1] + k1);
-  T phi2 = T(0), chi2 = T(0), psi2 = T(0);
+  T phi2 = T(1), chi2 = T(1), psi2 = T(1);
   if constexpr (DIM == 3) {
     phi2 = __ldg(fp.tab.kphi[2] + k2);
     chi2 = __ldg(fp.tab.kchi[2] + k2);
     psi2 = __ldg(fp.tab.kpsi[2] + k2);
   }
+  // Per-line products of the axis-1/axis-2 factors (2D: axis 1 only).
+  LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
 #pragma unroll
   for (int q = 0; q < 8; q++) {
     const int k0 = t + p0.T() * q;
@@ -207,10 +278,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
     cplx<T> u[DIM];
 #pragma unroll
     for (int c = 0; c < DIM; c++) u[c] = v[c][q];
-    if constexpr (DIM == 3)
-      stiffness3<T>(phi0, chi0, psi0, phi1, chi1, psi1, phi2, chi2, psi2, s, mu, u);
-    else
-      stiffness2<T>(phi0, chi0, psi0, phi1, chi1, psi1, s, mu, u);
+    stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
 #pragma unroll
     for (int c = 0; c < DIM; c++) v[c][q] = u[c];
   }
