@@ -23,7 +23,7 @@ struct bri17_op {
   void* stage_out;
   size_t stage_bytes;
   cudaStream_t copy_stream;   // host-API copies (lazy)
-  cudaEvent_t host_events[7]; // host-API pipeline events (lazy)
+  cudaEvent_t host_events[64]; // host-API pipeline events (lazy, reused)
 
   // Conjugate-gradient work space (lazy, owned by cg.cu).
   void* cg_work;
@@ -34,6 +34,8 @@ struct bri17_op {
 };
 
 namespace bri17gb {
+
+constexpr int kHostEvents = 64;
 
 // Scalar byte size of a handle's fields.
 inline size_t scalar_bytes(const bri17_op* op) {

@@ -894,7 +894,7 @@ extern "C" int bri17_op_destroy(bri17_op* op) {
   cudaFree(op->stage_out);
   if (op->copy_stream) {
     cudaStreamDestroy(op->copy_stream);
-    for (int i = 0; i < 7; i++) cudaEventDestroy(op->host_events[i]);
+    for (int i = 0; i < kHostEvents; i++) cudaEventDestroy(op->host_events[i]);
   }
   if (op->cg_work && op->cg_free) op->cg_free(op->cg_work);
   delete reinterpret_cast<PassTiming*>(op->timing);
@@ -970,23 +970,30 @@ extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
   return apply_stiffness_async(op, u, f, (cudaStream_t)stream);
 }
 
-// f = K u from host buffers, pipelined per component: the copy stream
-// uploads component c while the compute stream runs the forward passes of
-// component c-1, and downloads component c while the inverse passes of
-// component c+1 run.  Only the axis-0 pass needs all components at once.
+// f = K u from host buffers, pipelined in chunks of axis-0 planes: the
+// copy stream uploads chunk j while the compute stream runs the last-axis
+// and axis-1 passes of chunk j-1 (both only need whole planes), and
+// downloads chunk j while the inverse passes of chunk j+1 run.  Only the
+// axis-0 pass needs all of the field at once.
+constexpr int kHostChunksPerComp = 4;
+
 template <typename T>
 static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
                                 cudaStream_t st) {
   const Geometry& g = op->g;
   const int dim = g.dim;
-  const int64_t rows_per_comp = g.size / g.n[dim - 1];
-  const size_t cbytes = (size_t)g.size * sizeof(T);
+  const int n0 = g.n[0];
+  // Elements of one axis-0 plane: real field, spectrum rows, spectrum.
+  const int64_t plane_real = g.size / n0;
+  const int64_t plane_rows = plane_real / g.n[dim - 1];
+  const int64_t plane_spec = g.cspec / n0;
+  const int per = std::max(1, (n0 + kHostChunksPerComp - 1) / kHostChunksPerComp);
   const Tables<T>& tab = *reinterpret_cast<const Tables<T>*>(
       op->precision == BRI17_F64 ? (const void*)&op->tab64 : (const void*)&op->tab32);
   T* din = reinterpret_cast<T*>(op->stage_in);
   T* dout = reinterpret_cast<T*>(op->stage_out);
   cplx<T>* S = reinterpret_cast<cplx<T>*>(op->spec);
-  cudaEvent_t* ev = op->host_events;  // [0] start, [1..3] in, [4..6] out
+  cudaEvent_t* ev = op->host_events;
   BatchMask none;
   none.flags = nullptr;
   none.stride = 0;
@@ -995,20 +1002,27 @@ static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
   cudaStream_t cp = op->copy_stream;
   BRI17_CUDA_TRY(cudaEventRecord(ev[0], st));
   BRI17_CUDA_TRY(cudaStreamWaitEvent(cp, ev[0], 0));
+  int nev = 0;
+  auto next_event = [&]() { return ev[1 + (nev++ % (kHostEvents - 1))]; };
+  // Forward: per chunk, upload then last-axis (+ axis-1) passes.
   for (int c = 0; c < dim; c++) {
-    BRI17_CUDA_TRY(cudaMemcpyAsync(din + c * g.size, u_host + c * g.size, cbytes,
-                                   cudaMemcpyHostToDevice, cp));
-    BRI17_CUDA_TRY(cudaEventRecord(ev[1 + c], cp));
-  }
-  for (int c = 0; c < dim; c++) {
-    BRI17_CUDA_TRY(cudaStreamWaitEvent(st, ev[1 + c], 0));
-    {
-      PassScope ps(op, 0, st);
-      launch_rows_r2c<T>(g, din + c * g.size, S + c * g.cspec, rows_per_comp, tab, none, st);
-    }
-    if (dim == 3) {
-      PassScope ps(op, 1, st);
-      launch_axis1<T, false>(g, S + c * g.cspec, g.n[0], tab, none, st);
+    for (int p0 = 0; p0 < n0; p0 += per) {
+      const int np = std::min(per, n0 - p0);
+      const int64_t roff = c * g.size + p0 * plane_real;
+      BRI17_CUDA_TRY(cudaMemcpyAsync(din + roff, u_host + roff, np * plane_real * sizeof(T),
+                                     cudaMemcpyHostToDevice, cp));
+      cudaEvent_t e = next_event();
+      BRI17_CUDA_TRY(cudaEventRecord(e, cp));
+      BRI17_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
+      cplx<T>* Sc = S + c * g.cspec + p0 * plane_spec;
+      {
+        PassScope ps(op, 0, st);
+        launch_rows_r2c<T>(g, din + roff, Sc, np * plane_rows, tab, none, st);
+      }
+      if (dim == 3) {
+        PassScope ps(op, 1, st);
+        launch_axis1<T, false>(g, Sc, np, tab, none, st);
+      }
     }
   }
   FusedParams<T> fp = fused_params<T>(op, tab, kModeStiffness);
@@ -1021,19 +1035,26 @@ static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
       rc = launch_fused<T, 2, kModeStiffness>(g, S, 1, (int64_t)dim * g.cspec, fp, none, st);
   }
   if (rc != BRI17_OK) return rc;
+  // Inverse: per chunk, axis-1 (+ last-axis) passes then download.
   for (int c = 0; c < dim; c++) {
-    if (dim == 3) {
-      PassScope ps(op, 3, st);
-      launch_axis1<T, true>(g, S + c * g.cspec, g.n[0], tab, none, st);
+    for (int p0 = 0; p0 < n0; p0 += per) {
+      const int np = std::min(per, n0 - p0);
+      const int64_t roff = c * g.size + p0 * plane_real;
+      cplx<T>* Sc = S + c * g.cspec + p0 * plane_spec;
+      if (dim == 3) {
+        PassScope ps(op, 3, st);
+        launch_axis1<T, true>(g, Sc, np, tab, none, st);
+      }
+      {
+        PassScope ps(op, 4, st);
+        launch_rows_c2r<T>(g, Sc, dout + roff, np * plane_rows, tab, none, st);
+      }
+      cudaEvent_t e = next_event();
+      BRI17_CUDA_TRY(cudaEventRecord(e, st));
+      BRI17_CUDA_TRY(cudaStreamWaitEvent(cp, e, 0));
+      BRI17_CUDA_TRY(cudaMemcpyAsync(f_host + roff, dout + roff, np * plane_real * sizeof(T),
+                                     cudaMemcpyDeviceToHost, cp));
     }
-    {
-      PassScope ps(op, 4, st);
-      launch_rows_c2r<T>(g, S + c * g.cspec, dout + c * g.size, rows_per_comp, tab, none, st);
-    }
-    BRI17_CUDA_TRY(cudaEventRecord(ev[4 + c], st));
-    BRI17_CUDA_TRY(cudaStreamWaitEvent(cp, ev[4 + c], 0));
-    BRI17_CUDA_TRY(cudaMemcpyAsync(f_host + c * g.size, dout + c * g.size, cbytes,
-                                   cudaMemcpyDeviceToHost, cp));
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "operator launch");
@@ -1058,7 +1079,7 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
   }
   if (!op->copy_stream) {
     BRI17_CUDA_TRY(cudaStreamCreateWithFlags(&op->copy_stream, cudaStreamNonBlocking));
-    for (int i = 0; i < 7; i++)
+    for (int i = 0; i < kHostEvents; i++)
       BRI17_CUDA_TRY(cudaEventCreateWithFlags(&op->host_events[i], cudaEventDisableTiming));
   }
   int rc = ensure_spectrum(op, op->g.dim);
