@@ -970,12 +970,13 @@ extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
   return apply_stiffness_async(op, u, f, (cudaStream_t)stream);
 }
 
-// f = K u from host buffers, pipelined in chunks of axis-0 planes: the
+// f = K u from host buffers, pipelined in chunks of axis-0 planes (one
+// chunk per component: finer chunks leave the GPU under-filled): the
 // copy stream uploads chunk j while the compute stream runs the last-axis
 // and axis-1 passes of chunk j-1 (both only need whole planes), and
 // downloads chunk j while the inverse passes of chunk j+1 run.  Only the
 // axis-0 pass needs all of the field at once.
-constexpr int kHostChunksPerComp = 4;
+constexpr int kHostChunksPerComp = 1;  // finer chunks measured slower (launch tails)
 
 template <typename T>
 static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
