@@ -51,11 +51,12 @@ __device__ __forceinline__ int pad16(int p) { return p + (p >> 4); }
 // Line pitch (complex elements, odd so consecutive lines use distinct banks).
 __host__ __device__ __forceinline__ int pitch8(int n) { return n + n / 16 + 1; }
 
-template <typename T, int R, bool INV>
-__device__ __forceinline__ void stage8(cplx<T> (&v)[8], cplx<T>* buf, int t, int TT,
+// One radix-R stage with E elements per thread (E/R butterflies per thread).
+template <typename T, int R, int E, bool INV>
+__device__ __forceinline__ void stageE(cplx<T> (&v)[E], cplx<T>* buf, int t, int TT,
                                        int Ns, int n, const cplx<T>* __restrict__ tw,
                                        int tws, bool last) {
-  constexpr int M = 8 / R;
+  constexpr int M = E / R;
   const int tstep = (n / (Ns * R)) * tws;
 #pragma unroll
   for (int m = 0; m < M; m++) {
@@ -78,6 +79,13 @@ __device__ __forceinline__ void stage8(cplx<T> (&v)[8], cplx<T>* buf, int t, int
       for (int r = 0; r < R; r++) buf[pad16(d + r * Ns)] = a[r];
     }
   }
+}
+
+template <typename T, int R, bool INV>
+__device__ __forceinline__ void stage8(cplx<T> (&v)[8], cplx<T>* buf, int t, int TT,
+                                       int Ns, int n, const cplx<T>* __restrict__ tw,
+                                       int tws, bool last) {
+  stageE<T, R, 8, INV>(v, buf, t, TT, Ns, n, tw, tws, last);
 }
 
 // Transform one line held as v[q] = x[t + T q]; the result replaces v in the

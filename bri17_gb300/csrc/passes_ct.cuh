@@ -1,8 +1,12 @@
 // passes_ct.cuh -- launchers of the compile-time-length instances of the
 // power-of-two passes; passes_ct_f32.cu and passes_ct_f64.cu instantiate
 // them for one scalar type each (separate translation units build in
-// parallel).
+// parallel).  FP32 lines use 16 elements per thread (one shared-memory
+// exchange fewer for most lengths; FP32 registers allow it), FP64 lines 8
+// (three FP64 components of 16 would not fit the register file).
 #pragma once
+
+#include <algorithm>
 
 #include "passes_p2.cuh"
 
@@ -10,17 +14,38 @@ namespace bri17gb {
 
 #define BRI17_CT_CASES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
 
+// Elements per thread for scalar T and line length N (single-component
+// passes); the fused axis-0 pass holds DIM components per thread and uses 8.
+template <typename T, int N>
+struct CtE {
+  static constexpr int value = (sizeof(T) == 4 && N >= 16) ? 16 : 8;
+};
+constexpr int kFusedE = 8;
+
+// Rows per CTA for the last-axis passes: kP2Threads threads' worth, a power
+// of two dividing the rows of one batch entry when masked.
+inline int ct_rows_per_cta(int T, int64_t nrows, const BatchMask& mask) {
+  int rb = std::max(1, kP2Threads / T);
+  if (mask.flags)
+    while (rb > 1 && mask.unit % rb != 0) rb /= 2;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(rb, nrows));
+}
+
 template <typename T>
 bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx<T>* tw,
-                 int RB, size_t smem, BatchMask mask, cudaStream_t st) {
-  const unsigned grid = (unsigned)((nrows + RB - 1) / RB);
+                 BatchMask mask, cudaStream_t st) {
   switch (m) {
-#define CASE(N)                                                                      \
-  case N:                                                                            \
-    if (N > 512) return false;                                                       \
-    rows_r2c_p2<T, CtEng<N>><<<grid, (N / 8) * RB, smem, st>>>(x, X, nrows, H,       \
-                                                               CtEng<N>{}, tw, RB, mask); \
-    return true;
+#define CASE(N)                                                                       \
+  case N: {                                                                           \
+    if (N > 512) return false;                                                        \
+    constexpr int E = CtE<T, N>::value;                                               \
+    const int TT = N / E;                                                             \
+    const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
+    const size_t smem = (3 * N + 1 + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);       \
+    rows_r2c_p2<T, CtEng<N, E>><<<(unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st>>>( \
+        x, X, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
+    return true;                                                                      \
+  }
     BRI17_CT_CASES(CASE)
 #undef CASE
     default:
@@ -30,15 +55,19 @@ bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx
 
 template <typename T>
 bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx<T>* tw,
-                 int RB, size_t smem, BatchMask mask, cudaStream_t st) {
-  const unsigned grid = (unsigned)((nrows + RB - 1) / RB);
+                 BatchMask mask, cudaStream_t st) {
   switch (m) {
-#define CASE(N)                                                                      \
-  case N:                                                                            \
-    if (N > 512) return false;                                                       \
-    rows_c2r_p2<T, CtEng<N>><<<grid, (N / 8) * RB, smem, st>>>(X, x, nrows, H,       \
-                                                               CtEng<N>{}, tw, RB, mask); \
-    return true;
+#define CASE(N)                                                                       \
+  case N: {                                                                           \
+    if (N > 512) return false;                                                        \
+    constexpr int E = CtE<T, N>::value;                                               \
+    const int TT = N / E;                                                             \
+    const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
+    const size_t smem = (2 * N + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);           \
+    rows_c2r_p2<T, CtEng<N, E>><<<(unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st>>>( \
+        X, x, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
+    return true;                                                                      \
+  }
     BRI17_CT_CASES(CASE)
 #undef CASE
     default:
@@ -47,14 +76,20 @@ bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx
 }
 
 template <typename T, bool INV>
-bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int TB, dim3 grid, size_t smem,
-                 const cplx<T>* tw, BatchMask mask, cudaStream_t st) {
+bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw,
+                 BatchMask mask, cudaStream_t st) {
   switch (n) {
-#define CASE(N)                                                                       \
-  case N:                                                                             \
-    axis_c2c_p2<T, INV, CtEng<N>><<<grid, (N / 8) * TB, smem, st>>>(X, B, TB, CtEng<N>{}, \
-                                                                    tw, mask);        \
-    return true;
+#define CASE(N)                                                                        \
+  case N: {                                                                            \
+    constexpr int E = CtE<T, N>::value;                                                \
+    const int TT = N / E;                                                              \
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B));   \
+    const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
+    dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);                        \
+    axis_c2c_p2<T, INV, CtEng<N, E>><<<grid, TT * TB, smem, st>>>(X, B, TB, CtEng<N, E>{}, \
+                                                                  tw, mask);           \
+    return true;                                                                       \
+  }
     BRI17_CT_CASES(CASE)
 #undef CASE
     default:
@@ -64,14 +99,20 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int TB, dim3 grid, size_t smem,
 
 template <typename T, int DIM>
 bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t bstride,
-                        int TB, dim3 grid, size_t smem, const FusedParams<T>& fp,
-                        BatchMask mask, cudaStream_t st) {
+                        int batch, const FusedParams<T>& fp, BatchMask mask,
+                        cudaStream_t st) {
   switch (n0) {
-#define CASE(N)                                                                  \
-  case N:                                                                        \
-    axis0_stiffness_p2<T, DIM, CtEng<N>><<<grid, (N / 8) * TB, smem, st>>>(     \
-        X, P, cstride, bstride, TB, CtEng<N>{}, fp, mask);                      \
-    return true;
+#define CASE(N)                                                                        \
+  case N: {                                                                            \
+    constexpr int E = kFusedE;                                                         \
+    const int TT = N / E;                                                              \
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / TT, P)); \
+    const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
+    dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
+    axis0_stiffness_p2<T, DIM, CtEng<N, E>><<<grid, TT * TB, smem, st>>>(              \
+        X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                          \
+    return true;                                                                       \
+  }
     BRI17_CT_CASES(CASE)
 #undef CASE
     default:
@@ -81,39 +122,40 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
 
 template <typename T>
 void ct_set_smem_attrs_t(size_t max_smem) {
-#define CASE(N)                                                                              \
-  cudaFuncSetAttribute(rows_r2c_p2<T, CtEng<N>>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                       (int)max_smem);                                                       \
-  cudaFuncSetAttribute(rows_c2r_p2<T, CtEng<N>>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                       (int)max_smem);                                                       \
-  cudaFuncSetAttribute(axis_c2c_p2<T, false, CtEng<N>>,                                      \
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);          \
-  cudaFuncSetAttribute(axis_c2c_p2<T, true, CtEng<N>>,                                       \
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);          \
-  cudaFuncSetAttribute(axis0_stiffness_p2<T, 2, CtEng<N>>,                                   \
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);          \
-  cudaFuncSetAttribute(axis0_stiffness_p2<T, 3, CtEng<N>>,                                   \
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+#define CASE(N)                                                                        \
+  {                                                                                    \
+    constexpr int E = CtE<T, N>::value;                                                \
+    cudaFuncSetAttribute(rows_r2c_p2<T, CtEng<N, E>>,                                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(rows_c2r_p2<T, CtEng<N, E>>,                                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(axis_c2c_p2<T, false, CtEng<N, E>>,                           \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(axis_c2c_p2<T, true, CtEng<N, E>>,                            \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(axis0_stiffness_p2<T, 2, CtEng<N, kFusedE>>,                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(axis0_stiffness_p2<T, 3, CtEng<N, kFusedE>>,                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+  }
   BRI17_CT_CASES(CASE)
 #undef CASE
   cudaGetLastError();
 }
 
 #define BRI17_CT_INSTANTIATE(T)                                                             \
-  template bool ct_rows_r2c<T>(int, const T*, cplx<T>*, int64_t, int, const cplx<T>*, int, \
-                               size_t, BatchMask, cudaStream_t);                           \
-  template bool ct_rows_c2r<T>(int, const cplx<T>*, T*, int64_t, int, const cplx<T>*, int, \
-                               size_t, BatchMask, cudaStream_t);                           \
-  template bool ct_axis_c2c<T, false>(int, cplx<T>*, int64_t, int, dim3, size_t,            \
-                                      const cplx<T>*, BatchMask, cudaStream_t);             \
-  template bool ct_axis_c2c<T, true>(int, cplx<T>*, int64_t, int, dim3, size_t,             \
-                                     const cplx<T>*, BatchMask, cudaStream_t);              \
+  template bool ct_rows_r2c<T>(int, const T*, cplx<T>*, int64_t, int, const cplx<T>*,      \
+                               BatchMask, cudaStream_t);                                   \
+  template bool ct_rows_c2r<T>(int, const cplx<T>*, T*, int64_t, int, const cplx<T>*,      \
+                               BatchMask, cudaStream_t);                                   \
+  template bool ct_axis_c2c<T, false>(int, cplx<T>*, int64_t, int64_t, const cplx<T>*,      \
+                                      BatchMask, cudaStream_t);                             \
+  template bool ct_axis_c2c<T, true>(int, cplx<T>*, int64_t, int64_t, const cplx<T>*,       \
+                                     BatchMask, cudaStream_t);                              \
   template bool ct_axis0_stiffness<T, 2>(int, cplx<T>*, int64_t, int64_t, int64_t, int,     \
-                                         dim3, size_t, const FusedParams<T>&, BatchMask,    \
-                                         cudaStream_t);                                     \
+                                         const FusedParams<T>&, BatchMask, cudaStream_t);   \
   template bool ct_axis0_stiffness<T, 3>(int, cplx<T>*, int64_t, int64_t, int64_t, int,     \
-                                         dim3, size_t, const FusedParams<T>&, BatchMask,    \
-                                         cudaStream_t);                                     \
+                                         const FusedParams<T>&, BatchMask, cudaStream_t);   \
   template void ct_set_smem_attrs_t<T>(size_t);
 
 }  // namespace bri17gb

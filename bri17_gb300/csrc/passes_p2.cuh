@@ -13,6 +13,7 @@ namespace bri17gb {
 // Engine policies: the kernels below take either the runtime-plan engine
 // (any power-of-two length) or a compile-time-length engine.
 struct RtEng {
+  static constexpr int E = 8;
   Plan8 p;
   __device__ __forceinline__ int n() const { return p.n; }
   __device__ __forceinline__ int T() const { return p.T; }
@@ -23,14 +24,15 @@ struct RtEng {
   }
 };
 
-template <int N>
+template <int N, int EE = 8>
 struct CtEng {
+  static constexpr int E = EE;
   __device__ __forceinline__ constexpr int n() const { return N; }
-  __device__ __forceinline__ constexpr int T() const { return N / 8; }
+  __device__ __forceinline__ constexpr int T() const { return N / EE; }
   template <typename S, bool INV>
-  __device__ __forceinline__ void run(cplx<S> (&v)[8], cplx<S>* buf, int t,
+  __device__ __forceinline__ void run(cplx<S> (&v)[EE], cplx<S>* buf, int t,
                                       const cplx<S>* __restrict__ tw, int tws) const {
-    fft8_ct<S, N, INV>(v, buf, t, tw, tws);
+    fftE_ct<S, N, EE, INV>(v, buf, t, tw, tws);
   }
 };
 
@@ -59,15 +61,15 @@ __global__ void __launch_bounds__(kP2Threads)
     tw[i] = w;
     if (i <= m) twh[i] = mk<T>(T(0.5) * w.x, T(0.5) * w.y);
   }
-  cplx<T> v[8];
+  cplx<T> v[Eng::E];
   const cplx<T>* xc = reinterpret_cast<const cplx<T>*>(x) + row * m;
 #pragma unroll
-  for (int q = 0; q < 8; q++) v[q] = valid ? xc[t + TT * q] : mk<T>(T(0), T(0));
+  for (int q = 0; q < Eng::E; q++) v[q] = valid ? xc[t + TT * q] : mk<T>(T(0), T(0));
   __syncthreads();
   cplx<T>* buf = bufs + rb * pitch;
   pm.template run<T, false>(v, buf, t, tw, 2);
 #pragma unroll
-  for (int q = 0; q < 8; q++) buf[pad16(t + TT * q)] = v[q];
+  for (int q = 0; q < Eng::E; q++) buf[pad16(t + TT * q)] = v[q];
   __syncthreads();
   if (!valid) return;
   cplx<T>* out = X + row * H;
@@ -75,7 +77,7 @@ __global__ void __launch_bounds__(kP2Threads)
   // conj(Z_{m-k})); the 1/2 lives in the twh table and one fused
   // multiply-add per part.
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
+  for (int q = 0; q < Eng::E; q++) {
     const int k = t + TT * q;
     const cplx<T> zk = v[q];
     const cplx<T> zm = buf[pad16((m - k) & (m - 1))];
@@ -104,10 +106,10 @@ __global__ void __launch_bounds__(kP2Threads)
   const bool valid = rb < RB && row < nrows;
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
   __syncthreads();
-  cplx<T> v[8];
+  cplx<T> v[Eng::E];
   const cplx<T>* in = X + row * H;
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
+  for (int q = 0; q < Eng::E; q++) {
     const int k = t + TT * q;
     if (valid) {
       const cplx<T> xk = in[k];
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(kP2Threads)
   if (!valid) return;
   cplx<T>* xc = reinterpret_cast<cplx<T>*>(x) + row * m;
 #pragma unroll
-  for (int q = 0; q < 8; q++) xc[t + TT * q] = v[q];
+  for (int q = 0; q < Eng::E; q++) xc[t + TT * q] = v[q];
 }
 
 // Middle axis: complex [A][n][B], lines along n; TB consecutive inner
@@ -144,15 +146,15 @@ __global__ void __launch_bounds__(kP2Threads)
   const bool valid = b < B;
   cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b;
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
-  cplx<T> v[8];
+  cplx<T> v[Eng::E];
 #pragma unroll
-  for (int q = 0; q < 8; q++)
+  for (int q = 0; q < Eng::E; q++)
     v[q] = valid ? base[(int64_t)(t + p.T() * q) * B] : mk<T>(T(0), T(0));
   __syncthreads();
   p.template run<T, INV>(v, bufs + tb * pitch, t, tw, 1);
   if (!valid) return;
 #pragma unroll
-  for (int q = 0; q < 8; q++) base[(int64_t)(t + p.T() * q) * B] = v[q];
+  for (int q = 0; q < Eng::E; q++) base[(int64_t)(t + p.T() * q) * B] = v[q];
 }
 
 // Products of one spectrum line's axis-1/axis-2 factors of
@@ -241,11 +243,11 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   }
   for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
   cplx<T>* buf = bufs + tb * pitch;
-  cplx<T> v[DIM][8];
+  cplx<T> v[DIM][Eng::E];
 #pragma unroll
   for (int c = 0; c < DIM; c++)
 #pragma unroll
-    for (int q = 0; q < 8; q++)
+    for (int q = 0; q < Eng::E; q++)
       v[c][q] = valid ? base[c * cstride + (int64_t)(t + p0.T() * q) * P]
                       : mk<T>(T(0), T(0));
   __syncthreads();
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   // Per-line products of the axis-1/axis-2 factors (2D: axis 1 only).
   LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
+  for (int q = 0; q < Eng::E; q++) {
     const int k0 = t + p0.T() * q;
     const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
             psi0 = __ldg(fp.tab.kpsi[0] + k0);
@@ -288,7 +290,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
 #pragma unroll
   for (int c = 0; c < DIM; c++)
 #pragma unroll
-    for (int q = 0; q < 8; q++) base[c * cstride + (int64_t)(t + p0.T() * q) * P] = v[c][q];
+    for (int q = 0; q < Eng::E; q++) base[c * cstride + (int64_t)(t + p0.T() * q) * P] = v[c][q];
 }
 
 }  // namespace bri17gb
@@ -296,21 +298,22 @@ __global__ void __launch_bounds__(kP2FusedThreads)
 namespace bri17gb {
 
 // Launchers of the compile-time-length kernels (passes_ct.cuh, instantiated
-// in passes_ct_f32.cu / passes_ct_f64.cu).  Each returns false, launching
-// nothing, when the length has no compile-time instance.
+// in passes_ct_f32.cu / passes_ct_f64.cu).  Each picks its own block
+// geometry and returns false, launching nothing, when the length has no
+// compile-time instance.
 template <typename T>
 bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx<T>* tw,
-                 int RB, size_t smem, BatchMask mask, cudaStream_t st);
+                 BatchMask mask, cudaStream_t st);
 template <typename T>
 bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx<T>* tw,
-                 int RB, size_t smem, BatchMask mask, cudaStream_t st);
+                 BatchMask mask, cudaStream_t st);
 template <typename T, bool INV>
-bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int TB, dim3 grid, size_t smem,
-                 const cplx<T>* tw, BatchMask mask, cudaStream_t st);
+bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw,
+                 BatchMask mask, cudaStream_t st);
 template <typename T, int DIM>
 bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t bstride,
-                        int TB, dim3 grid, size_t smem, const FusedParams<T>& fp,
-                        BatchMask mask, cudaStream_t st);
+                        int batch, const FusedParams<T>& fp, BatchMask mask,
+                        cudaStream_t st);
 void ct_set_smem_attrs(size_t max_smem);
 
 }  // namespace bri17gb
