@@ -232,7 +232,7 @@ static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
     if (ct_rows_r2c<T>(p.n, x, X, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
     const size_t smem = (3 * p.n + 1 + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
-    rows_r2c_p2<T, RtEng><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
+    launch_pdl(rows_r2c_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st, 
         x, X, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
     return BRI17_OK;
   }
@@ -242,7 +242,7 @@ static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
   const int rows = rows_per_cta(m, nrows, mask.unit, mask.flags != nullptr);
   size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)rows * pitch * sizeof(cplx<T>);
   const int64_t grid = (nrows + rows - 1) / rows;
-  rows_r2c<T><<<(unsigned)grid, kThreads, smem, st>>>(x, X, nrows, n, g.H, g.plan_row,
+  launch_pdl(rows_r2c<T>, (unsigned)grid, kThreads, smem, st, x, X, nrows, n, g.H, g.plan_row,
                                                       tab.tw[g.dim - 1], rows, pitch, mask);
   return BRI17_OK;
 }
@@ -256,7 +256,7 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
     if (ct_rows_c2r<T>(p.n, X, x, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
     const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
-    rows_c2r_p2<T, RtEng><<<(unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st>>>(
+    launch_pdl(rows_c2r_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st, 
         X, x, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
     return BRI17_OK;
   }
@@ -266,7 +266,7 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
   const int rows = rows_per_cta(m, nrows, mask.unit, mask.flags != nullptr);
   size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)rows * pitch * sizeof(cplx<T>);
   const int64_t grid = (nrows + rows - 1) / rows;
-  rows_c2r<T><<<(unsigned)grid, kThreads, smem, st>>>(X, x, nrows, n, g.H, g.plan_row,
+  launch_pdl(rows_c2r<T>, (unsigned)grid, kThreads, smem, st, X, x, nrows, n, g.H, g.plan_row,
                                                       tab.tw[g.dim - 1], rows, pitch, mask);
   return BRI17_OK;
 }
@@ -280,7 +280,7 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
     const int TB = (int)std::min<int64_t>(kP2Threads / p.T, g.H);
     const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.H + TB - 1) / TB), (unsigned)nouter);
-    axis_c2c_p2<T, INV, RtEng><<<grid, p.T * TB, smem, st>>>(X, g.H, TB, RtEng{p}, tab.tw[1],
+    launch_pdl(axis_c2c_p2<T, INV, RtEng>, grid, p.T * TB, smem, st, X, g.H, TB, RtEng{p}, tab.tw[1],
                                                              mask);
     return BRI17_OK;
   }
@@ -290,7 +290,7 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
   int TB = (int)std::min<int64_t>(B, std::max(4, std::min(32, kTileElems / n)));
   size_t smem = n * sizeof(cplx<T>) + 2 * (size_t)TB * pitch * sizeof(cplx<T>);
   dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);
-  axis_c2c<T, INV><<<grid, kThreads, smem, st>>>(X, n, B, TB, pitch, g.plan[1], tab.tw[1],
+  launch_pdl(axis_c2c<T, INV>, grid, kThreads, smem, st, X, n, B, TB, pitch, g.plan[1], tab.tw[1],
                                                 mask);
   return BRI17_OK;
 }
@@ -310,7 +310,7 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / p.T, g.P));
     const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
-    axis0_stiffness_p2<T, DIM, RtEng><<<grid, p.T * TB, smem, st>>>(
+    launch_pdl(axis0_stiffness_p2<T, DIM, RtEng>, grid, p.T * TB, smem, st, 
         X, g.P, g.cspec, bstride, TB, RtEng{p}, fp, mask);
     return BRI17_OK;
   }
@@ -330,7 +330,7 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
   TB = (int)std::min<int64_t>(TB, g.P);
   size_t smem = n0 * sizeof(cplx<T>) + (size_t)TB * per_line;
   dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
-  axis0_fused<T, DIM, MODE><<<grid, kThreads, smem, st>>>(
+  launch_pdl(axis0_fused<T, DIM, MODE>, grid, kThreads, smem, st, 
       X, n0, g.P, g.cspec, bstride, TB, pitch, g.plan[0], fp, mask);
   return BRI17_OK;
 }

@@ -18,6 +18,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "pdl.cuh"
 
 namespace bri17gb {
 
@@ -66,9 +67,11 @@ __global__ void __launch_bounds__(kThreads)
   const bool even = (n % 2) == 0;
   const int m = even ? n / 2 : n;
   const int64_t row0 = (int64_t)blockIdx.x * rows_per_cta;
-  if (mask.skip(row0)) return;
   const int nr = (int)min((int64_t)rows_per_cta, nrows - row0);
+  pdl_launch_dependents();
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
+  pdl_wait();
+  if (mask.skip(row0)) return;
   if (even) {
     const cplx<T>* xc = reinterpret_cast<const cplx<T>*>(x) + row0 * m;
     for (int f = threadIdx.x; f < nr * m; f += blockDim.x) {
@@ -116,10 +119,12 @@ __global__ void __launch_bounds__(kThreads)
   const bool even = (n % 2) == 0;
   const int m = even ? n / 2 : n;
   const int64_t row0 = (int64_t)blockIdx.x * rows_per_cta;
-  if (mask.skip(row0)) return;
   const int nr = (int)min((int64_t)rows_per_cta, nrows - row0);
+  pdl_launch_dependents();
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
   __syncthreads();
+  pdl_wait();
+  if (mask.skip(row0)) return;
   const cplx<T>* in = X + row0 * H;
   if (even) {
     for (int f = threadIdx.x; f < nr * m; f += blockDim.x) {
@@ -178,11 +183,13 @@ __global__ void __launch_bounds__(kThreads)
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* a = tw + n;
   cplx<T>* b = a + TB * pitch;
-  if (mask.skip(blockIdx.y)) return;
   const int64_t b0 = (int64_t)blockIdx.x * TB;
   const int nb = (int)min((int64_t)TB, B - b0);
   cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b0;
+  pdl_launch_dependents();
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
+  pdl_wait();
+  if (mask.skip(blockIdx.y)) return;
   for (int f = threadIdx.x; f < n * nb; f += blockDim.x) {
     const int i = f / nb;
     const int tb = f - i * nb;
@@ -292,16 +299,18 @@ __global__ void __launch_bounds__(kThreads)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* buf = tw + n0;  // CMAX + 1 buffers of TB * pitch
-  if (mask.skip(blockIdx.y)) return;
   const int64_t b0 = (int64_t)blockIdx.x * TB;
   const int nb = (int)min((int64_t)TB, P - b0);
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b0;
+  pdl_launch_dependents();
+  for (int t = threadIdx.x; t < n0; t += blockDim.x) tw[t] = fp.tab.tw[0][t];
+  pdl_wait();
+  if (mask.skip(blockIdx.y)) return;
   T s = fp.s, mu = fp.mu;
   if (fp.mat) {
     s = fp.mat[2 * blockIdx.y];
     mu = fp.mat[2 * blockIdx.y + 1];
   }
-  for (int t = threadIdx.x; t < n0; t += blockDim.x) tw[t] = fp.tab.tw[0][t];
   for (int c = 0; c < CIN; c++) {
     cplx<T>* a = buf + c * TB * pitch;
     const cplx<T>* src = base + c * cstride;

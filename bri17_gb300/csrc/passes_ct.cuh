@@ -1,9 +1,8 @@
 // passes_ct.cuh -- launchers of the compile-time-length instances of the
 // power-of-two passes; passes_ct_f32.cu and passes_ct_f64.cu instantiate
 // them for one scalar type each (separate translation units build in
-// parallel).  FP32 lines use 16 elements per thread (one shared-memory
-// exchange fewer for most lengths; FP32 registers allow it), FP64 lines 8
-// (three FP64 components of 16 would not fit the register file).
+// parallel).  Every launch carries the programmatic-dependent-launch
+// attribute (see pdl.cuh).
 #pragma once
 
 #include <algorithm>
@@ -18,7 +17,9 @@ namespace bri17gb {
 // passes); the fused axis-0 pass holds DIM components per thread and uses 8.
 template <typename T, int N>
 struct CtE {
-  static constexpr int value = (sizeof(T) == 4 && N >= 16) ? 16 : 8;
+  // 16 elements per thread was measured slower than 8 for the FP32 row
+  // passes (fewer threads per row, longer dependency chains): 8 throughout.
+  static constexpr int value = 8;
 };
 constexpr int kFusedE = 8;
 
@@ -42,7 +43,7 @@ bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
     const size_t smem = (3 * N + 1 + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);       \
-    rows_r2c_p2<T, CtEng<N, E>><<<(unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st>>>( \
+    launch_pdl(rows_r2c_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         x, X, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
     return true;                                                                      \
   }
@@ -64,7 +65,7 @@ bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
     const size_t smem = (2 * N + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);           \
-    rows_c2r_p2<T, CtEng<N, E>><<<(unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st>>>( \
+    launch_pdl(rows_c2r_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         X, x, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
     return true;                                                                      \
   }
@@ -86,7 +87,7 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B));   \
     const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
     dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);                        \
-    axis_c2c_p2<T, INV, CtEng<N, E>><<<grid, TT * TB, smem, st>>>(X, B, TB, CtEng<N, E>{}, \
+    launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E>>, grid, TT * TB, smem, st, X, B, TB, CtEng<N, E>{}, \
                                                                   tw, mask);           \
     return true;                                                                       \
   }
@@ -109,7 +110,7 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / TT, P)); \
     const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
     dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
-    axis0_stiffness_p2<T, DIM, CtEng<N, E>><<<grid, TT * TB, smem, st>>>(              \
+    launch_pdl(axis0_stiffness_p2<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,               \
         X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                          \
     return true;                                                                       \
   }

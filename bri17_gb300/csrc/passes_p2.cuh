@@ -7,6 +7,7 @@
 #include "fft8.cuh"
 #include "fft8_ct.cuh"
 #include "passes.cuh"
+#include "pdl.cuh"
 
 namespace bri17gb {
 
@@ -52,15 +53,17 @@ __global__ void __launch_bounds__(kP2Threads)
   cplx<T>* twh = tw + n;        // W_n^k / 2, k in [0, m]
   cplx<T>* bufs = twh + m + 1;
   const int64_t row0 = (int64_t)blockIdx.x * RB;
-  if (mask.skip(row0)) return;
   const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
+  pdl_launch_dependents();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const cplx<T> w = tw_g[i];
     tw[i] = w;
     if (i <= m) twh[i] = mk<T>(T(0.5) * w.x, T(0.5) * w.y);
   }
+  pdl_wait();
+  if (mask.skip(row0)) return;
   cplx<T> v[Eng::E];
   const cplx<T>* xc = reinterpret_cast<const cplx<T>*>(x) + row * m;
 #pragma unroll
@@ -100,12 +103,14 @@ __global__ void __launch_bounds__(kP2Threads)
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
   const int64_t row0 = (int64_t)blockIdx.x * RB;
-  if (mask.skip(row0)) return;
   const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
+  pdl_launch_dependents();
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
   __syncthreads();
+  pdl_wait();
+  if (mask.skip(row0)) return;
   cplx<T> v[Eng::E];
   const cplx<T>* in = X + row * H;
 #pragma unroll
@@ -140,12 +145,14 @@ __global__ void __launch_bounds__(kP2Threads)
   const int pitch = pitch8(n);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
-  if (mask.skip(blockIdx.y)) return;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
   const int64_t b = (int64_t)blockIdx.x * TB + tb;
   const bool valid = b < B;
   cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b;
+  pdl_launch_dependents();
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  pdl_wait();
+  if (mask.skip(blockIdx.y)) return;
   cplx<T> v[Eng::E];
 #pragma unroll
   for (int q = 0; q < Eng::E; q++)
@@ -231,19 +238,21 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   const int pitch = pitch8(n0);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n0;
-  if (mask.skip(blockIdx.y)) return;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
   const int64_t b = (int64_t)blockIdx.x * TB + tb;
   const bool valid = b < P;
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
+  pdl_launch_dependents();
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  pdl_wait();
+  if (mask.skip(blockIdx.y)) return;
   T s = fp.s, mu = fp.mu;
   if (fp.mat) {
     s = fp.mat[2 * blockIdx.y];
     mu = fp.mat[2 * blockIdx.y + 1];
   }
-  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
-  cplx<T>* buf = bufs + tb * pitch;
   cplx<T> v[DIM][Eng::E];
+  cplx<T>* buf = bufs + tb * pitch;
 #pragma unroll
   for (int c = 0; c < DIM; c++)
 #pragma unroll
