@@ -291,7 +291,9 @@ def run_operator(args, precision="f64"):
     for i in range(args.warmup):
         hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
     torch.cuda.synchronize()
-    L.bri17_op_set_pass_timing(hooke.handle, 1)
+    # Official timed region: K applications back to back, CUDA events on the
+    # launching stream, nothing between the launches (the passes overlap
+    # through programmatic dependent launch).
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
@@ -308,7 +310,20 @@ def run_operator(args, precision="f64"):
         torch.distributed.barrier()
     clocks = sampler.stop()
     ms_total = e0.elapsed_time(e1)
+    value, t_max = aggregate_replicas(ms_total, dof, args.steps, device="cuda")
+    # Per-kernel durations: the same K applications again with the library
+    # recording CUDA events around every pass launch (events between the
+    # launches also serialise the passes, so this loop is slower).
     import ctypes
+    L.bri17_op_set_pass_timing(hooke.handle, 1)
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for i in range(args.steps):
+        hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_with_events = e2.elapsed_time(e3) / max(1, args.steps)
     pms = (ctypes.c_double * 5)()
     pn = (ctypes.c_int64 * 5)()
     npass = ctypes.c_int()
@@ -316,7 +331,6 @@ def run_operator(args, precision="f64"):
     L.bri17_op_set_pass_timing(hooke.handle, 0)
     passes = {L.bri17_pass_name(i).decode(): {"ms_total": pms[i], "launches": pn[i]}
               for i in range(5) if pn[i] > 0}
-    value, t_max = aggregate_replicas(ms_total, dof, args.steps, device="cuda")
     # Correctness of the timed output (first set) against a fresh apply.
     check = hooke.apply_stiffness(us[0])
     assert torch.equal(check, fs[0]) or args.steps == 0
@@ -381,7 +395,9 @@ def run_operator(args, precision="f64"):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": precision, "data": "synthetic", "config": config_of(w, ws, precision),
         "roofline": roof, "e2e": e2e, "gpu_launches": sum(p["launches"] for p in passes.values()),
-        "clocks": clocks, "passes": passes, **extra,
+        "gpu_launches_note": "launches per timed region (5 passes x K applications)",
+        "clocks": clocks, "passes": passes, "ms_per_step_with_pass_events": ms_with_events,
+        **extra,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         times = cpu_reference_apply_time(w, 1, 2)
