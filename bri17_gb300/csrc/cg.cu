@@ -26,10 +26,8 @@ __global__ void __launch_bounds__(kRedThreads)
     k_dot_pq(const T* __restrict__ p, const T* __restrict__ q, int64_t n,
              CgState* st, double* partials) {
   if (!st->active) return;
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    v += (double)p[i] * (double)q[i];
+  const double v = vdot<T>(p, q, n, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                           (int64_t)gridDim.x * blockDim.x);
   double tot;
   if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
       threadIdx.x == 0) {
@@ -50,15 +48,9 @@ __global__ void __launch_bounds__(kRedThreads)
              const T* __restrict__ q, int64_t n, CgState* st,
              double* partials) {
   if (!st->active) return;
-  const T a = (T)st->alpha;
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] += a * p[i];
-    const T ri = r[i] - a * q[i];
-    r[i] = ri;
-    v += (double)ri * (double)ri;
-  }
+  const double v = vupdate<T>(x, r, p, q, (T)st->alpha, n,
+                              (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                              (int64_t)gridDim.x * blockDim.x);
   double tot;
   if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
       threadIdx.x == 0) {
@@ -80,10 +72,8 @@ __global__ void __launch_bounds__(kRedThreads)
     k_pupdate(T* __restrict__ p, const T* __restrict__ r, int64_t n,
               const CgState* st) {
   if (!st->active) return;
-  const T b = (T)st->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = r[i] + b * p[i];
+  vpupdate<T>(p, r, (T)st->beta, n, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+              (int64_t)gridDim.x * blockDim.x);
 }
 
 // aux = a . b

@@ -77,6 +77,134 @@ __device__ __forceinline__ bool last_block_total(double v, double* partials,
 }
 
 
+// 16-byte vectors of the CG streams: float4 / double2.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int W = 4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+template <typename T>
+__device__ __forceinline__ T vget(const typename Vec16<T>::type& v, int i) {
+  return reinterpret_cast<const T*>(&v)[i];
+}
+template <typename T>
+__device__ __forceinline__ void vset(typename Vec16<T>::type& v, int i, T x) {
+  reinterpret_cast<T*>(&v)[i] = x;
+}
+
+// The CG vector kernels below stream their operands as 16-byte vectors, two
+// per thread per trip (several independent loads in flight per thread), and
+// finish the n mod W tail element-wise.  n is the length of one vector.
+// Operands that are not all 16-byte aligned (slot offsets of odd-sized grids
+// in a batch) take the element-wise loop for everything.
+__device__ __forceinline__ bool aligned16(const void* a, const void* b, const void* c = nullptr,
+                                          const void* d = nullptr) {
+  return ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+           reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(d)) &
+          15u) == 0;
+}
+
+// sum p.q (FP64 accumulation) of one vector.
+template <typename T>
+__device__ __forceinline__ double vdot(const T* __restrict__ p, const T* __restrict__ q,
+                                       int64_t n, int64_t tid, int64_t nthreads) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::W;
+  const int64_t nv = aligned16(p, q) ? n / W : 0;
+  const V* pv = reinterpret_cast<const V*>(p);
+  const V* qv = reinterpret_cast<const V*>(q);
+  double a0 = 0.0, a1 = 0.0;
+  int64_t i = tid;
+  for (; i + nthreads < nv; i += 2 * nthreads) {
+    const V p0 = pv[i], q0 = qv[i], p1 = pv[i + nthreads], q1 = qv[i + nthreads];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      a0 += (double)vget<T>(p0, k) * (double)vget<T>(q0, k);
+      a1 += (double)vget<T>(p1, k) * (double)vget<T>(q1, k);
+    }
+  }
+  for (; i < nv; i += nthreads) {
+    const V p0 = pv[i], q0 = qv[i];
+#pragma unroll
+    for (int k = 0; k < W; k++) a0 += (double)vget<T>(p0, k) * (double)vget<T>(q0, k);
+  }
+  for (int64_t j = nv * W + tid; j < n; j += nthreads) a0 += (double)p[j] * (double)q[j];
+  return a0 + a1;
+}
+
+// x += a p; r -= a q; returns sum r.r (FP64 accumulation).
+template <typename T>
+__device__ __forceinline__ double vupdate(T* __restrict__ x, T* __restrict__ r,
+                                          const T* __restrict__ p, const T* __restrict__ q,
+                                          T a, int64_t n, int64_t tid, int64_t nthreads) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::W;
+  const int64_t nv = aligned16(x, r, p, q) ? n / W : 0;
+  V* xv = reinterpret_cast<V*>(x);
+  V* rv = reinterpret_cast<V*>(r);
+  const V* pv = reinterpret_cast<const V*>(p);
+  const V* qv = reinterpret_cast<const V*>(q);
+  double acc = 0.0;
+  for (int64_t i = tid; i < nv; i += nthreads) {
+    V xi = xv[i], ri = rv[i];
+    const V pi = pv[i], qi = qv[i];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      vset<T>(xi, k, vget<T>(xi, k) + a * vget<T>(pi, k));
+      const T rk = vget<T>(ri, k) - a * vget<T>(qi, k);
+      vset<T>(ri, k, rk);
+      acc += (double)rk * (double)rk;
+    }
+    xv[i] = xi;
+    rv[i] = ri;
+  }
+  for (int64_t j = nv * W + tid; j < n; j += nthreads) {
+    x[j] += a * p[j];
+    const T rk = r[j] - a * q[j];
+    r[j] = rk;
+    acc += (double)rk * (double)rk;
+  }
+  return acc;
+}
+
+// p = r + b p.
+template <typename T>
+__device__ __forceinline__ void vpupdate(T* __restrict__ p, const T* __restrict__ r, T b,
+                                         int64_t n, int64_t tid, int64_t nthreads) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::W;
+  const int64_t nv = aligned16(p, r) ? n / W : 0;
+  V* pv = reinterpret_cast<V*>(p);
+  const V* rv = reinterpret_cast<const V*>(r);
+  int64_t i = tid;
+  for (; i + nthreads < nv; i += 2 * nthreads) {
+    V p0 = pv[i], p1 = pv[i + nthreads];
+    const V r0 = rv[i], r1 = rv[i + nthreads];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+      vset<T>(p0, k, vget<T>(r0, k) + b * vget<T>(p0, k));
+      vset<T>(p1, k, vget<T>(r1, k) + b * vget<T>(p1, k));
+    }
+    pv[i] = p0;
+    pv[i + nthreads] = p1;
+  }
+  for (; i < nv; i += nthreads) {
+    V p0 = pv[i];
+    const V r0 = rv[i];
+#pragma unroll
+    for (int k = 0; k < W; k++) vset<T>(p0, k, vget<T>(r0, k) + b * vget<T>(p0, k));
+    pv[i] = p0;
+  }
+  for (int64_t j = nv * W + tid; j < n; j += nthreads) p[j] = r[j] + b * p[j];
+}
+
 // Ends iteration for states whose update kernel asked to pause: runs after
 // the search-direction update, so a paused CG resumes with a consistent p.
 static __global__ void k_apply_pause(CgState* sts, int count) {

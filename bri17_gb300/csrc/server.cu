@@ -114,12 +114,9 @@ __global__ void __launch_bounds__(kRedThreads)
               CgState* sts, double* partials) {
   CgState* st = sts + blockIdx.y;
   if (!st->active) return;
-  const float* pz = p + blockIdx.y * n;
-  const float* qz = q + blockIdx.y * n;
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    v += (double)pz[i] * (double)qz[i];
+  const double v = vdot<float>(p + blockIdx.y * n, q + blockIdx.y * n, n,
+                               (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                               (int64_t)gridDim.x * blockDim.x);
   double tot;
   bool last;
   slot_block_total(v, partials + blockIdx.y * kRedMaxBlocks, &st->counter, gridDim.x,
@@ -142,15 +139,9 @@ __global__ void __launch_bounds__(kRedThreads)
   CgState* st = sts + blockIdx.y;
   if (!st->active) return;
   const int64_t o = blockIdx.y * n;
-  const float a = (float)st->alpha;
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    x[o + i] += a * p[o + i];
-    const float ri = r[o + i] - a * q[o + i];
-    r[o + i] = ri;
-    v += (double)ri * (double)ri;
-  }
+  const double v = vupdate<float>(x + o, r + o, p + o, q + o, (float)st->alpha, n,
+                                  (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                                  (int64_t)gridDim.x * blockDim.x);
   double tot;
   bool last;
   slot_block_total(v, partials + blockIdx.y * kRedMaxBlocks, &st->counter, gridDim.x,
@@ -177,10 +168,9 @@ __global__ void __launch_bounds__(kRedThreads)
   const CgState* st = sts + blockIdx.y;
   if (!st->active) return;
   const int64_t o = blockIdx.y * n;
-  const float b = (float)st->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    p[o + i] = r[o + i] + b * p[o + i];
+  vpupdate<float>(p + o, r + o, (float)st->beta, n,
+                  (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                  (int64_t)gridDim.x * blockDim.x);
 }
 
 // --- per-slot helpers (one slot, 1-D grids) --------------------------------

@@ -29,7 +29,8 @@ def _requests(rng, n, sides):
 def test_server_results_equal_solo_solves_and_oracle():
     from bri17_gb300.server import Server
     rng = np.random.default_rng(3)
-    reqs = _requests(rng, 9, [16, 24, (20, 16, 12)])
+    # (15, 15, 15) puts odd slot offsets in its bucket (unaligned vectors).
+    reqs = _requests(rng, 10, [16, 24, (20, 16, 12), (15, 15, 15)])
     srv = Server(memory_budget_bytes=2 << 30, slots_per_bucket=4)
     ids = [srv.submit(*r, tol=TOL) for r in reqs]
     results = {r["id"]: r for r in srv.run_until_idle()}
