@@ -256,11 +256,11 @@ def run_reference(args):
 
 def config_of(w, ngpus, precision="f64"):
     shape = w["shape"]
-    return {"workload": f"operator f = K u, 3D hexahedral periodic grid "
-                        f"{shape[0]}x{shape[1]}x{shape[2]}, h=1/{shape[0]}, "
+    return {"workload": f"operator f = K u, periodic grid "
+                        f"{'x'.join(map(str, shape))}, h=1/{shape[0]}, "
                         f"mu={w['mu']} nu={w['nu']}, {precision.upper()}, u~N(0,1) seed "
                         f"{w['seed']} mean-free",
-            "grid": list(shape), "dof_per_step": 3 * int(np.prod(shape)),
+            "grid": list(shape), "dof_per_step": len(shape) * int(np.prod(shape)),
             "parallelism": f"replicas x{ngpus}",
             "l2": "inputs rotate over buffer sets larger than L2"}
 
@@ -274,7 +274,10 @@ def run_operator(args, precision="f64"):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    w = WORKLOAD_128
+    w = dict(WORKLOAD_128)
+    if args.shape:
+        w["shape"] = tuple(int(n) for n in args.shape.split("x"))
+        w["L"] = (1.0,) * len(w["shape"])
     shape = w["shape"]
     dim = len(shape)
     dof = dim * int(np.prod(shape))
@@ -365,7 +368,7 @@ def run_operator(args, precision="f64"):
                            "apply_device": t_max / max(1, args.steps)}
 
     hbm_peak, peak_kind = peaks()
-    cspec = shape[0] * shape[1] * (shape[2] // 2 + 1)
+    cspec = int(np.prod(shape[:-1])) * (shape[-1] // 2 + 1)
     pb = pass_bytes(dim, dof, cspec, dim, scalar)
     dom = max(passes, key=lambda k: passes[k]["ms_total"]) if passes else None
     roof = None
@@ -652,6 +655,8 @@ def main():
     ap.add_argument("--workload", default="operator",
                     choices=["operator", "operator_f32", "cg", "aniso", "serve"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shape", default="",
+                    help="operator workloads: grid other than 128x128x128 (e.g. 256x256x256)")
     ap.add_argument("--no-oracle", action="store_true")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--slots", type=int, default=8)

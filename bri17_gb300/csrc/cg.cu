@@ -734,6 +734,8 @@ extern "C" int bri17_cg_solve(bri17_op* op, const double* b, double* x,
     set_error("tol must be > 0, max_iterations >= 0, mode PLAIN, MIXED or MIXED_RESTART");
     return info->status = BRI17_ERR_INVALID_ARGUMENT;
   }
+  const int dc = check_device(op);
+  if (dc != BRI17_OK) return info->status = dc;
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return info->status = cuda_fail(e, "cudaStreamSynchronize");
   int rc;

@@ -42,6 +42,9 @@ inline size_t scalar_bytes(const bri17_op* op) {
   return op->precision == BRI17_F64 ? sizeof(double) : sizeof(float);
 }
 
+// BRI17_OK when the current CUDA device is the handle's device.
+int check_device(const bri17_op* op);
+
 // Grow the spectrum buffer to `comps` components.
 int ensure_spectrum(bri17_op* op, int comps);
 

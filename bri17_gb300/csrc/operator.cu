@@ -30,6 +30,19 @@ static int invalid(const char* msg) {
   return BRI17_ERR_INVALID_ARGUMENT;
 }
 
+// A handle's device memory lives on the device that was current when it was
+// created; calls must be made with that device current.
+int check_device(const bri17_op* op) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != op->device) {
+    set_error("the current CUDA device differs from the handle's device");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  return BRI17_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Plans.
 
@@ -925,6 +938,10 @@ extern "C" int bri17_op_set_material(bri17_op* op, double mu, double nu) {
 extern "C" int bri17_modal_stiffness_batch(const bri17_op* op, const int* k,
                                            int64_t n, void* K, void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (n < 0) return invalid("negative count");
   if (n == 0) return BRI17_OK;
   if (!k || !K) return invalid("null pointer");
@@ -939,6 +956,10 @@ extern "C" int bri17_modal_strain_displacement_batch(const bri17_op* op,
                                                      const int* k, int64_t n,
                                                      void* B, void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (n < 0) return invalid("negative count");
   if (n == 0) return BRI17_OK;
   if (!k || !B) return invalid("null pointer");
@@ -953,6 +974,10 @@ extern "C" int bri17_modal_eigenstress_to_opposite_strain_batch(
     const bri17_op* op, const int* k, int64_t n, const void* tau, void* eta,
     void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (n < 0) return invalid("negative count");
   if (n == 0) return BRI17_OK;
   if (!k || !tau || !eta) return invalid("null pointer");
@@ -966,6 +991,10 @@ extern "C" int bri17_modal_eigenstress_to_opposite_strain_batch(
 extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
                                      void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (!u || !f) return invalid("null pointer");
   return apply_stiffness_async(op, u, f, (cudaStream_t)stream);
 }
@@ -1066,6 +1095,10 @@ static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
 extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
                                           void* f_host, void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (!u_host || !f_host) return invalid("null pointer");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t bytes = (size_t)op->g.dim * op->g.size * scalar_bytes(op);
@@ -1093,6 +1126,10 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
 extern "C" int bri17_apply_strain(bri17_op* op, const void* u, void* eps,
                                   void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (!u || !eps) return invalid("null pointer");
   const int sym = op->g.dim == 2 ? 3 : 6;
   int rc = ensure_spectrum(op, sym);
@@ -1108,6 +1145,10 @@ extern "C" int bri17_apply_strain(bri17_op* op, const void* u, void* eps,
 extern "C" int bri17_eigenstress_rhs(bri17_op* op, const void* tau, void* b,
                                      void* stream) {
   if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
   if (!tau || !b) return invalid("null pointer");
   const int sym = op->g.dim == 2 ? 3 : 6;
   int rc = ensure_spectrum(op, sym);

@@ -33,7 +33,9 @@
  *     function says otherwise.  "_host" pointers are host memory; those
  *     functions synchronise `stream` before returning.
  *   - A handle is externally synchronised (one thread at a time); distinct
- *     handles may be used concurrently.
+ *     handles may be used concurrently.  A handle belongs to the CUDA device
+ *     that was current when it was created: calls made with another device
+ *     current return BRI17_ERR_INVALID_ARGUMENT.
  */
 #ifndef BRI17_GB300_H_
 #define BRI17_GB300_H_
