@@ -318,6 +318,21 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
   constexpr int CMAX = CIN > COUT ? CIN : COUT;
   if (MODE == kModeStiffness && g.use_p8[0]) {
     const Plan8& p = g.p8[0];
+    // The staged form (one component in registers) when its tile fits the
+    // shared memory: more warps per SM.  BRI17_FUSED_FORM=registers|staged
+    // selects a form explicitly (for measurements).
+    static const int form = [] {
+      const char* e = getenv("BRI17_FUSED_FORM");
+      if (!e) return 0;
+      return strcmp(e, "registers") == 0 ? 1 : strcmp(e, "staged") == 0 ? 2 : 0;
+    }();
+    const int TT = p.n / 8;
+    const int64_t TBs = std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, g.P));
+    const size_t smem_staged = (p.n + (size_t)(1 + DIM) * TBs * pitch8(p.n)) * sizeof(cplx<T>);
+    const bool staged = form == 2 || (form == 0 && smem_staged <= 120 * 1024);
+    if (staged &&
+        ct_axis0_stiffness_staged<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
+      return BRI17_OK;
     if (ct_axis0_stiffness<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
       return BRI17_OK;
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / p.T, g.P));

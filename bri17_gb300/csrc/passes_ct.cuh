@@ -121,6 +121,32 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
   }
 }
 
+// Staged form: TB lines per CTA with kP2Threads threads (at least 8
+// consecutive lines for 64-byte segments), 1 + 1 + DIM lines of shared
+// memory per line of the tile.
+template <typename T, int DIM>
+bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
+                               int64_t bstride, int batch, const FusedParams<T>& fp,
+                               BatchMask mask, cudaStream_t st) {
+  switch (n0) {
+#define CASE(N)                                                                        \
+  case N: {                                                                            \
+    constexpr int E = 8;                                                               \
+    const int TT = N / E;                                                              \
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, P));   \
+    const size_t smem = (N + (size_t)(1 + DIM) * TB * pitch8(N)) * sizeof(cplx<T>);     \
+    dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
+    launch_pdl(axis0_stiffness_staged<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,   \
+               X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                   \
+    return true;                                                                       \
+  }
+    BRI17_CT_CASES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
 template <typename T>
 void ct_set_smem_attrs_t(size_t max_smem) {
 #define CASE(N)                                                                        \
@@ -137,6 +163,10 @@ void ct_set_smem_attrs_t(size_t max_smem) {
     cudaFuncSetAttribute(axis0_stiffness_p2<T, 2, CtEng<N, kFusedE>>,                  \
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
     cudaFuncSetAttribute(axis0_stiffness_p2<T, 3, CtEng<N, kFusedE>>,                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(axis0_stiffness_staged<T, 2, CtEng<N, 8>>,                    \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
+    cudaFuncSetAttribute(axis0_stiffness_staged<T, 3, CtEng<N, 8>>,                    \
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);  \
   }
   BRI17_CT_CASES(CASE)
@@ -157,6 +187,12 @@ void ct_set_smem_attrs_t(size_t max_smem) {
                                          const FusedParams<T>&, BatchMask, cudaStream_t);   \
   template bool ct_axis0_stiffness<T, 3>(int, cplx<T>*, int64_t, int64_t, int64_t, int,     \
                                          const FusedParams<T>&, BatchMask, cudaStream_t);   \
+  template bool ct_axis0_stiffness_staged<T, 2>(int, cplx<T>*, int64_t, int64_t, int64_t,   \
+                                                int, const FusedParams<T>&, BatchMask,      \
+                                                cudaStream_t);                              \
+  template bool ct_axis0_stiffness_staged<T, 3>(int, cplx<T>*, int64_t, int64_t, int64_t,   \
+                                                int, const FusedParams<T>&, BatchMask,      \
+                                                cudaStream_t);                              \
   template void ct_set_smem_attrs_t<T>(size_t);
 
 }  // namespace bri17gb

@@ -306,6 +306,93 @@ __global__ void __launch_bounds__(kP2FusedThreads)
 
 namespace bri17gb {
 
+// Axis 0, fused stiffness, shared-memory staged: the same computation as
+// axis0_stiffness_p2 with one component in registers at a time.  Each
+// component's forward transform is parked in shared memory at the thread's
+// own positions (no barrier needed: a thread reads back only what it wrote),
+// K(k) u(k) runs from there, and the inverse transforms read it back.  Half
+// the registers of the register-resident form, so twice the warps per SM.
+template <typename T, int DIM, class Eng>
+__global__ void __launch_bounds__(kP2Threads)
+    axis0_stiffness_staged(cplx<T>* __restrict__ X, int64_t P, int64_t cstride,
+                           int64_t bstride, int TB, Eng p0, FusedParams<T> fp,
+                           BatchMask mask) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n0 = p0.n();
+  const int pitch = pitch8(n0);
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* exch = tw + n0;                      // TB exchange lines
+  cplx<T>* stash = exch + (size_t)TB * pitch;   // DIM x TB staged lines
+  const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
+  const int64_t b = (int64_t)blockIdx.x * TB + tb;
+  const bool valid = b < P;
+  cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
+  pdl_launch_dependents();
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  pdl_wait();
+  if (mask.skip(blockIdx.y)) return;
+  T s = fp.s, mu = fp.mu;
+  if (fp.mat) {
+    s = fp.mat[2 * blockIdx.y];
+    mu = fp.mat[2 * blockIdx.y + 1];
+  }
+  __syncthreads();
+  cplx<T>* buf = exch + tb * pitch;
+  cplx<T> v[Eng::E];
+#pragma unroll 1
+  for (int c = 0; c < DIM; c++) {
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++)
+      v[q] = valid ? base[c * cstride + (int64_t)(t + p0.T() * q) * P] : mk<T>(T(0), T(0));
+    p0.template run<T, false>(v, buf, t, tw, 1);
+    cplx<T>* st = stash + ((size_t)c * TB + tb) * pitch;
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++) st[pad16(t + p0.T() * q)] = v[q];
+  }
+  int k1 = 0, k2 = 0;
+  if (valid) {
+    if constexpr (DIM == 3) {
+      k1 = (int)(b / fp.H);
+      k2 = (int)(b - (int64_t)k1 * fp.H);
+    } else {
+      k1 = (int)b;
+    }
+  }
+  const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
+          psi1 = __ldg(fp.tab.kpsi[1] + k1);
+  T phi2 = T(1), chi2 = T(1), psi2 = T(1);
+  if constexpr (DIM == 3) {
+    phi2 = __ldg(fp.tab.kphi[2] + k2);
+    chi2 = __ldg(fp.tab.kchi[2] + k2);
+    psi2 = __ldg(fp.tab.kpsi[2] + k2);
+  }
+  const LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
+#pragma unroll 2
+  for (int q = 0; q < Eng::E; q++) {
+    const int k0 = t + p0.T() * q;
+    const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
+            psi0 = __ldg(fp.tab.kpsi[0] + k0);
+    const int pos = pad16(k0);
+    cplx<T> u[DIM];
+#pragma unroll
+    for (int c = 0; c < DIM; c++) u[c] = stash[((size_t)c * TB + tb) * pitch + pos];
+    stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
+#pragma unroll
+    for (int c = 0; c < DIM; c++) stash[((size_t)c * TB + tb) * pitch + pos] = u[c];
+  }
+#pragma unroll 1
+  for (int c = 0; c < DIM; c++) {
+    const cplx<T>* st = stash + ((size_t)c * TB + tb) * pitch;
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++) v[q] = st[pad16(t + p0.T() * q)];
+    p0.template run<T, true>(v, buf, t, tw, 1);
+    if (valid) {
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) base[c * cstride + (int64_t)(t + p0.T() * q) * P] = v[q];
+    }
+  }
+}
+
 // Launchers of the compile-time-length kernels (passes_ct.cuh, instantiated
 // in passes_ct_f32.cu / passes_ct_f64.cu).  Each picks its own block
 // geometry and returns false, launching nothing, when the length has no
@@ -323,6 +410,10 @@ template <typename T, int DIM>
 bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t bstride,
                         int batch, const FusedParams<T>& fp, BatchMask mask,
                         cudaStream_t st);
+template <typename T, int DIM>
+bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
+                               int64_t bstride, int batch, const FusedParams<T>& fp,
+                               BatchMask mask, cudaStream_t st);
 void ct_set_smem_attrs(size_t max_smem);
 
 }  // namespace bri17gb
