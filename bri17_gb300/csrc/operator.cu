@@ -318,19 +318,15 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
   constexpr int CMAX = CIN > COUT ? CIN : COUT;
   if (MODE == kModeStiffness && g.use_p8[0]) {
     const Plan8& p = g.p8[0];
-    // The staged form (one component in registers) when its tile fits the
-    // shared memory: more warps per SM.  BRI17_FUSED_FORM=registers|staged
-    // selects a form explicitly (for measurements).
-    static const int form = [] {
+    // Form chosen per handle (fused_form, autotuned at creation for FP32);
+    // BRI17_FUSED_FORM=registers|staged overrides it (for measurements).
+    static const int env_form = [] {
       const char* e = getenv("BRI17_FUSED_FORM");
-      if (!e) return 0;
-      return strcmp(e, "registers") == 0 ? 1 : strcmp(e, "staged") == 0 ? 2 : 0;
+      if (!e) return -1;
+      return strcmp(e, "registers") == 0 ? 0 : strcmp(e, "staged") == 0 ? 1 : -1;
     }();
-    const int TT = p.n / 8;
-    const int64_t TBs = std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, g.P));
-    const size_t smem_staged = (p.n + (size_t)(1 + DIM) * TBs * pitch8(p.n)) * sizeof(cplx<T>);
-    const bool staged = form == 2 || (form == 0 && smem_staged <= 120 * 1024);
-    if (staged &&
+    const int form = env_form >= 0 ? env_form : fp.form;
+    if (form == 1 &&
         ct_axis0_stiffness_staged<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
       return BRI17_OK;
     if (ct_axis0_stiffness<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
@@ -375,6 +371,7 @@ static FusedParams<T> fused_params(const bri17_op* op, const Tables<T>& tab,
   fp.mu = (T)(op->mu * op->corr);
   fp.corr = mode == kModeStrain ? (T)(1.0 / (double)op->g.size) : (T)op->corr;
   fp.mat = nullptr;
+  fp.form = op->fused_form;
   return fp;
 }
 
@@ -567,6 +564,55 @@ int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
                                           (double*)b, batch, spec, nullptr, st);
   return run_pipeline<float, kModeRhs>(op, op->tab32, (const float*)tau,
                                        (float*)b, batch, spec, nullptr, st);
+}
+
+// Times the two forms of the FP32 axis-0 stiffness pass on the handle's own
+// spectrum buffer (its contents are irrelevant to the timing) and keeps the
+// faster: the staged form wins where the register form's tile is too narrow
+// for full memory segments, the register form elsewhere.
+void autotune_fused_form(bri17_op* op) {
+  const Geometry& g = op->g;
+  cudaStream_t st;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int best_form = 0;
+  for (int form = 0; form < 2; form++) {
+    op->fused_form = form;
+    FusedParams<float> fp = fused_params<float>(op, op->tab32, kModeStiffness);
+    BatchMask none;
+    none.flags = nullptr;
+    none.stride = 0;
+    none.unit = 1;
+    cplx<float>* S = reinterpret_cast<cplx<float>*>(op->spec);
+    float ms = 0.f;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, st);
+      if (g.dim == 3)
+        launch_fused<float, 3, kModeStiffness>(g, S, 1, (int64_t)g.dim * g.cspec, fp, none, st);
+      else
+        launch_fused<float, 2, kModeStiffness>(g, S, 1, (int64_t)g.dim * g.cspec, fp, none, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0) ms += t;  // the first run warms up
+    }
+    if (ms < best) {
+      best = ms;
+      best_form = form;
+    }
+  }
+  op->fused_form = best_form;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -908,6 +954,7 @@ extern "C" int bri17_op_create(int dim, const int* shape, const double* L,
     set_smem_attrs<double>();
   else
     set_smem_attrs<float>();
+  if (precision == BRI17_F32 && g.use_p8[0]) autotune_fused_form(op);
   *out = op;
   return BRI17_OK;
 }

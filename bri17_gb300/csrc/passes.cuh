@@ -48,6 +48,7 @@ struct FusedParams {
   T mu;             // mu * corr
   T corr;           // normalisation of strain / rhs modes
   const T* mat;     // optional per-batch (s, mu) pairs, overriding s, mu
+  int form;         // power-of-two axis-0 stiffness pass: 0 registers, 1 staged
 };
 
 // ---------------------------------------------------------------------------
