@@ -51,19 +51,6 @@ __device__ __forceinline__ int pad16(int p) { return p + (p >> 4); }
 // Line pitch (complex elements, odd so consecutive lines use distinct banks).
 __host__ __device__ __forceinline__ int pitch8(int n) { return n + n / 16 + 1; }
 
-// Line pitch of a tile whose warps step `s` elements along a line, then to
-// the next line (s = 32 / lines per tile for the strided-axis passes, s =
-// threads per row for the row passes).  With M complex elements per 128-byte
-// bank row, a pitch = s (mod M) puts a warp's 32 lanes on every bank the
-// minimum number of times; s >= 32 keeps a warp within one line.
-__host__ __device__ __forceinline__ int tile_pitch(int n, int s, int csize) {
-  const int base = n + n / 16 + 1;
-  if (s >= 32 || s < 1) return base;
-  const int M = 128 / csize;
-  const int r = (base + M - 1) / M * M;
-  return r + (s % M);
-}
-
 // One radix-R stage with E elements per thread (E/R butterflies per thread).
 template <typename T, int R, int E, bool INV>
 __device__ __forceinline__ void stageE(cplx<T> (&v)[E], cplx<T>* buf, int t, int TT,

@@ -244,8 +244,7 @@ static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
     const Plan8& p = g.p8_row;
     if (ct_rows_r2c<T>(p.n, x, X, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
-    const size_t smem =
-        (3 * p.n + 1 + (size_t)rb * tile_pitch(p.n, p.T, sizeof(cplx<T>))) * sizeof(cplx<T>);
+    const size_t smem = (3 * p.n + 1 + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
     launch_pdl(rows_r2c_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st, 
         x, X, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
     return BRI17_OK;
@@ -269,8 +268,7 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
     const Plan8& p = g.p8_row;
     if (ct_rows_c2r<T>(p.n, X, x, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
-    const size_t smem =
-        (2 * p.n + (size_t)rb * tile_pitch(p.n, p.T, sizeof(cplx<T>))) * sizeof(cplx<T>);
+    const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
     launch_pdl(rows_c2r_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st, 
         X, x, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
     return BRI17_OK;
@@ -293,8 +291,7 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
     const Plan8& p = g.p8[1];
     if (ct_axis_c2c<T, INV>(p.n, X, g.H, nouter, tab.tw[1], mask, st)) return BRI17_OK;
     const int TB = (int)std::min<int64_t>(kP2Threads / p.T, g.H);
-    const size_t smem =
-        (p.n + (size_t)TB * tile_pitch(p.n, 32 / TB, sizeof(cplx<T>))) * sizeof(cplx<T>);
+    const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.H + TB - 1) / TB), (unsigned)nouter);
     launch_pdl(axis_c2c_p2<T, INV, RtEng>, grid, p.T * TB, smem, st, X, g.H, TB, RtEng{p}, tab.tw[1],
                                                              mask);
@@ -335,8 +332,7 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
     if (ct_axis0_stiffness<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
       return BRI17_OK;
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / p.T, g.P));
-    const size_t smem =
-        (p.n + (size_t)TB * tile_pitch(p.n, 32 / TB, sizeof(cplx<T>))) * sizeof(cplx<T>);
+    const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
     launch_pdl(axis0_stiffness_p2<T, DIM, RtEng>, grid, p.T * TB, smem, st, 
         X, g.P, g.cspec, bstride, TB, RtEng{p}, fp, mask);

@@ -42,7 +42,7 @@ bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx
     constexpr int E = CtE<T, N>::value;                                               \
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
-    const size_t smem = (3 * N + 1 + (size_t)rb * tile_pitch(N, TT, sizeof(cplx<T>))) * sizeof(cplx<T>);       \
+    const size_t smem = (3 * N + 1 + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);       \
     launch_pdl(rows_r2c_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         x, X, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
     return true;                                                                      \
@@ -64,7 +64,7 @@ bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx
     constexpr int E = CtE<T, N>::value;                                               \
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
-    const size_t smem = (2 * N + (size_t)rb * tile_pitch(N, TT, sizeof(cplx<T>))) * sizeof(cplx<T>);           \
+    const size_t smem = (2 * N + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);           \
     launch_pdl(rows_c2r_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         X, x, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
     return true;                                                                      \
@@ -85,7 +85,7 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw
     constexpr int E = CtE<T, N>::value;                                                \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B));   \
-    const size_t smem = (N + (size_t)TB * tile_pitch(N, 32 / TB, sizeof(cplx<T>))) * sizeof(cplx<T>);                \
+    const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
     dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);                        \
     launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E>>, grid, TT * TB, smem, st, X, B, TB, CtEng<N, E>{}, \
                                                                   tw, mask);           \
@@ -108,7 +108,7 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
     constexpr int E = kFusedE;                                                         \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / TT, P)); \
-    const size_t smem = (N + (size_t)TB * tile_pitch(N, 32 / TB, sizeof(cplx<T>))) * sizeof(cplx<T>);                \
+    const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
     dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
     launch_pdl(axis0_stiffness_p2<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,               \
         X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                          \
@@ -134,7 +134,7 @@ bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
     constexpr int E = 8;                                                               \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, P));   \
-    const size_t smem = (N + (size_t)(1 + DIM) * TB * tile_pitch(N, 32 / TB, sizeof(cplx<T>))) * sizeof(cplx<T>);     \
+    const size_t smem = (N + (size_t)(1 + DIM) * TB * pitch8(N)) * sizeof(cplx<T>);     \
     dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
     launch_pdl(axis0_stiffness_staged<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,   \
                X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                   \

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(kP2Threads)
                 Eng pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
-  const int pitch = tile_pitch(m, TT, (int)sizeof(cplx<T>));
+  const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* twh = tw + n;        // W_n^k / 2, k in [0, m]
   cplx<T>* bufs = twh + m + 1;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kP2Threads)
                 Eng pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
-  const int pitch = tile_pitch(m, TT, (int)sizeof(cplx<T>));
+  const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
   const int64_t row0 = (int64_t)blockIdx.x * RB;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kP2Threads)
                 const cplx<T>* __restrict__ tw_g, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = p.n();
-  const int pitch = tile_pitch(n, 32 / TB, (int)sizeof(cplx<T>));
+  const int pitch = pitch8(n);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
                        BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = p0.n();
-  const int pitch = tile_pitch(n0, 32 / TB, (int)sizeof(cplx<T>));
+  const int pitch = pitch8(n0);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n0;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(kP2Threads)
                            BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = p0.n();
-  const int pitch = tile_pitch(n0, 32 / TB, (int)sizeof(cplx<T>));
+  const int pitch = pitch8(n0);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* exch = tw + n0;                      // TB exchange lines
   cplx<T>* stash = exch + (size_t)TB * pitch;   // DIM x TB staged lines
