@@ -51,6 +51,16 @@ __device__ __forceinline__ int pad16(int p) { return p + (p >> 4); }
 // Line pitch (complex elements, odd so consecutive lines use distinct banks).
 __host__ __device__ __forceinline__ int pitch8(int n) { return n + n / 16 + 1; }
 
+// Pitch of lines accessed only in natural order with warp lanes stepping
+// across the TB lines first: lines stagger by 32 / TB elements modulo the M
+// complex elements of a 128-byte bank row, so a warp's 32 lanes use every
+// bank the minimum number of times.
+__host__ __device__ __forceinline__ int stash_pitch(int n, int TB, int csize) {
+  const int M = 128 / csize;
+  const int s = TB >= 1 && TB <= 32 ? 32 / TB : 1;
+  return (n + M - 1) / M * M + (s % M == 0 ? M / 2 + 1 : s % M);
+}
+
 // One radix-R stage with E elements per thread (E/R butterflies per thread).
 template <typename T, int R, int E, bool INV>
 __device__ __forceinline__ void stageE(cplx<T> (&v)[E], cplx<T>* buf, int t, int TT,

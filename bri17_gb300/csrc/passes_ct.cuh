@@ -134,7 +134,7 @@ bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
     constexpr int E = 8;                                                               \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, P));   \
-    const size_t smem = (N + (size_t)(1 + DIM) * TB * pitch8(N)) * sizeof(cplx<T>);     \
+    const size_t smem = (N + (size_t)TB * pitch8(N) + (size_t)DIM * TB * stash_pitch(N, TB, sizeof(cplx<T>))) * sizeof(cplx<T>);     \
     dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
     launch_pdl(axis0_stiffness_staged<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,   \
                X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                   \

@@ -320,6 +320,10 @@ __global__ void __launch_bounds__(kP2Threads)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = p0.n();
   const int pitch = pitch8(n0);
+  // Staged lines are only read and written at a thread's own positions,
+  // lanes stepping across the TB lines first: their pitch staggers lines by
+  // 32 / TB elements modulo one 128-byte bank row.
+  const int spitch = stash_pitch(n0, TB, (int)sizeof(cplx<T>));
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* exch = tw + n0;                      // TB exchange lines
   cplx<T>* stash = exch + (size_t)TB * pitch;   // DIM x TB staged lines
@@ -345,9 +349,9 @@ __global__ void __launch_bounds__(kP2Threads)
     for (int q = 0; q < Eng::E; q++)
       v[q] = valid ? base[c * cstride + (int64_t)(t + p0.T() * q) * P] : mk<T>(T(0), T(0));
     p0.template run<T, false>(v, buf, t, tw, 1);
-    cplx<T>* st = stash + ((size_t)c * TB + tb) * pitch;
+    cplx<T>* st = stash + ((size_t)c * TB + tb) * spitch;
 #pragma unroll
-    for (int q = 0; q < Eng::E; q++) st[pad16(t + p0.T() * q)] = v[q];
+    for (int q = 0; q < Eng::E; q++) st[t + p0.T() * q] = v[q];
   }
   int k1 = 0, k2 = 0;
   if (valid) {
@@ -372,19 +376,18 @@ __global__ void __launch_bounds__(kP2Threads)
     const int k0 = t + p0.T() * q;
     const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
             psi0 = __ldg(fp.tab.kpsi[0] + k0);
-    const int pos = pad16(k0);
     cplx<T> u[DIM];
 #pragma unroll
-    for (int c = 0; c < DIM; c++) u[c] = stash[((size_t)c * TB + tb) * pitch + pos];
+    for (int c = 0; c < DIM; c++) u[c] = stash[((size_t)c * TB + tb) * spitch + k0];
     stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
 #pragma unroll
-    for (int c = 0; c < DIM; c++) stash[((size_t)c * TB + tb) * pitch + pos] = u[c];
+    for (int c = 0; c < DIM; c++) stash[((size_t)c * TB + tb) * spitch + k0] = u[c];
   }
 #pragma unroll 1
   for (int c = 0; c < DIM; c++) {
-    const cplx<T>* st = stash + ((size_t)c * TB + tb) * pitch;
+    const cplx<T>* st = stash + ((size_t)c * TB + tb) * spitch;
 #pragma unroll
-    for (int q = 0; q < Eng::E; q++) v[q] = st[pad16(t + p0.T() * q)];
+    for (int q = 0; q < Eng::E; q++) v[q] = st[t + p0.T() * q];
     p0.template run<T, true>(v, buf, t, tw, 1);
     if (valid) {
 #pragma unroll
