@@ -126,6 +126,45 @@ int main(int argc, char** argv) {
     std::printf("exception: %s\n", e.what());
     return 1;
   }
+  // T = float instantiation of the header API: the FP32 operator
+  // agrees with the FP64 one to FP32 accuracy, and the per-mode methods
+  // return the FP64 values rounded to float.
+  {
+    bri17::CartesianGrid<float, 3> g32{{8, 6, 10}, {1.f, 0.75f, 1.25f}};
+    bri17::CartesianGrid<double, 3> g64{{8, 6, 10}, {1.0, 0.75, 1.25}};
+    bri17::Hooke<float, 3> h32{1.5f, 0.3f, g32};
+    bri17::Hooke<double, 3> h64{1.5, 0.3, g64};
+    const int n = 3 * g64.size;
+    std::vector<double> u64(n), f64(n), f32d(n);
+    std::vector<float> u32(n), f32(n);
+    unsigned s = 12345u;
+    for (int i = 0; i < n; i++) {
+      s = s * 1103515245u + 12345u;
+      u32[i] = (float)((s >> 8) % 2001) / 1000.f - 1.f;
+      u64[i] = u32[i];
+    }
+    h64.apply_stiffness_host(u64.data(), f64.data());
+    h32.apply_stiffness_host(u32.data(), f32.data());
+    double num = 0, den = 0;
+    for (int i = 0; i < n; i++) {
+      num += (f32[i] - f64[i]) * (f32[i] - f64[i]);
+      den += f64[i] * f64[i];
+    }
+    const double rel = std::sqrt(num / den);
+    int k[3] = {3, 2, 7};
+    std::complex<float> K32[9];
+    std::complex<double> K64[9];
+    h32.modal_stiffness(k, K32);
+    h64.modal_stiffness(k, K64);
+    bool modal_ok = true;
+    for (int i = 0; i < 9; i++)
+      modal_ok = modal_ok && K32[i] == std::complex<float>(K64[i]);
+    const bool ok = rel <= 2e-5 && modal_ok;
+    std::printf("Hooke<float,3>: operator rel err %.2e vs FP64, modal %s: %s\n", rel,
+                modal_ok ? "equal" : "differ", ok ? "passed" : "FAILED");
+    passed += ok;
+    total++;
+  }
   std::printf("%d of %d sections passed\n", passed, total);
   return passed == total && total > 0 ? 0 : 1;
 }

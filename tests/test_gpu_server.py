@@ -105,3 +105,20 @@ def test_submit_validation():
     res = srv.run_until_idle()
     assert res[0]["status"] == 0 and np.all(srv.result(rid) == 0)
     srv.close()
+
+
+def test_idle_bucket_released_when_memory_is_needed():
+    """With a budget that holds one bucket, a second geometry is admitted
+    after the first one's requests finish (its bucket is released)."""
+    from bri17_gb300.server import Server
+    rng = np.random.default_rng(6)
+    a = _requests(rng, 2, [24])
+    b = _requests(rng, 2, [(20, 16, 12)])
+    srv = Server(memory_budget_bytes=80 << 20, slots_per_bucket=2)
+    ids = [srv.submit(*r, tol=TOL) for r in a + b]
+    results = {r["id"]: r for r in srv.run_until_idle()}
+    assert all(results[i]["status"] == 0 for i in ids)
+    # The second geometry was admitted only after the first finished.
+    assert min(results[i]["admit_time_s"] for i in ids[2:]) >= \
+        max(results[i]["finish_time_s"] for i in ids[:2]) - 1e-6
+    srv.close()

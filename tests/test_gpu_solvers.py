@@ -97,3 +97,51 @@ def test_mixed_reliable_keeps_fp64_iteration_count(shape, nu):
     assert mixed["status"] == 0 and plain["status"] == 0
     assert mixed["iterations"] <= 1.3 * plain["iterations"] + 16, (mixed, plain)
     assert mixed["outer_iterations"] >= 2
+
+
+@pytest.mark.parametrize("shape", [(12, 10), (16, 12, 10), (5, 6, 7)])
+def test_f32_handle_strain_and_rhs(shape):
+    """The strain map and the eigenstress right-hand side on an FP32 handle
+    (generic and power-of-two paths) agree with the FP64 oracle to FP32
+    accuracy."""
+    import torch
+    L = (1.0,) * len(shape)
+    h, ho = pair(shape, L, 1.2, 0.25, precision="f32")
+    rng = np.random.default_rng(13)
+    sym = 3 if len(shape) == 2 else 6
+    u = rng.standard_normal((len(shape),) + shape)
+    tau = rng.standard_normal((sym,) + shape)
+    eps = h.apply_strain(to_dev(u, torch.float32)).double().cpu().numpy()
+    b = h.eigenstress_rhs(to_dev(tau, torch.float32)).double().cpu().numpy()
+    assert rel_l2(eps, O.apply_strain(ho, u)) <= 2e-5
+    assert rel_l2(b, O.eigenstress_rhs(ho, tau)) <= 2e-5
+
+
+def test_handle_info_and_modal_batch_on_f32_handle(golden_modal):
+    import ctypes
+
+    from bri17_gb300 import _lib
+    c = golden_modal[3]
+    h, _ = pair(c["shape"], c["L"], c["mu"], c["nu"], precision="f32")
+    K = h.modal_stiffness_batch(c["k"]).cpu().numpy().reshape(len(c["k"]), -1)
+    inr = np.all((c["k"] >= 0) & (c["k"] < np.array(c["shape"])), axis=1)
+    # The per-mode API computes in FP64 whatever the handle's field precision.
+    assert np.array_equal(K[inr].view(np.float64), c["K"][inr].view(np.float64))
+    size, ws = ctypes.c_int64(), ctypes.c_int64()
+    assert _lib.load().bri17_op_info(h.handle, ctypes.byref(size), ctypes.byref(ws)) == 0
+    n = c["shape"]
+    assert size.value == int(np.prod(n))
+    assert ws.value == 3 * n[0] * n[1] * (n[2] // 2 + 1) * 8
+
+
+def test_wrong_device_and_dtype_are_rejected():
+    import torch
+
+    from bri17_gb300._lib import Bri17Error
+    h, _ = pair((8, 8, 8), (1.0, 1.0, 1.0), 1.0, 0.3)
+    with pytest.raises(TypeError):
+        h.apply_stiffness(torch.zeros((3, 8, 8, 8), dtype=torch.float32, device="cuda"))
+    with pytest.raises(ValueError):
+        h.apply_stiffness(torch.zeros((3, 8, 8, 7), dtype=torch.float64, device="cuda"))
+    with pytest.raises(Bri17Error):
+        h.set_material(1.0, 0.5)
