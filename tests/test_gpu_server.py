@@ -112,9 +112,11 @@ def test_idle_bucket_released_when_memory_is_needed():
     after the first one's requests finish (its bucket is released)."""
     from bri17_gb300.server import Server
     rng = np.random.default_rng(6)
-    a = _requests(rng, 2, [24])
-    b = _requests(rng, 2, [(20, 16, 12)])
-    srv = Server(memory_budget_bytes=80 << 20, slots_per_bucket=2)
+    # A 48^3 bucket of 2 slots needs about 52 MB, a 40^3 one about 30 MB:
+    # a 70 MB budget holds either, not both.
+    a = _requests(rng, 2, [48])
+    b = _requests(rng, 2, [40])
+    srv = Server(memory_budget_bytes=70 << 20, slots_per_bucket=2)
     ids = [srv.submit(*r, tol=TOL) for r in a + b]
     results = {r["id"]: r for r in srv.run_until_idle()}
     assert all(results[i]["status"] == 0 for i in ids)
