@@ -132,8 +132,8 @@ int main(int argc, char** argv) {
   {
     bri17::CartesianGrid<float, 3> g32{{8, 6, 10}, {1.f, 0.75f, 1.25f}};
     bri17::CartesianGrid<double, 3> g64{{8, 6, 10}, {1.0, 0.75, 1.25}};
-    bri17::Hooke<float, 3> h32{1.5f, 0.3f, g32};
-    bri17::Hooke<double, 3> h64{1.5, 0.3, g64};
+    bri17::Hooke<float, 3> h32{1.5f, 0.25f, g32};  // nu exact in float and double
+    bri17::Hooke<double, 3> h64{1.5, 0.25, g64};
     const int n = 3 * g64.size;
     std::vector<double> u64(n), f64(n), f32d(n);
     std::vector<float> u32(n), f32(n);
