@@ -111,7 +111,16 @@ __device__ __forceinline__ bool aligned16(const void* a, const void* b, const vo
           15u) == 0;
 }
 
-// sum p.q (FP64 accumulation) of one vector.
+// Per-thread accumulator type of the vector reductions: a thread sums its
+// share (a few dozen terms) in the vectors' own precision and hands one
+// partial to the FP64 block/grid reduction.  FP32 streams thus never touch
+// the FP64 pipe per element (on GB300 it runs at 1/64 of the FP32 rate:
+// converting and accumulating every element in FP64 made a 50 M-element dot
+// product FP64-bound at 4x the time of the memory traffic).
+template <typename T>
+using Acc = T;
+
+// sum p.q of one vector.
 template <typename T>
 __device__ __forceinline__ double vdot(const T* __restrict__ p, const T* __restrict__ q,
                                        int64_t n, int64_t tid, int64_t nthreads) {
@@ -120,26 +129,31 @@ __device__ __forceinline__ double vdot(const T* __restrict__ p, const T* __restr
   const int64_t nv = aligned16(p, q) ? n / W : 0;
   const V* pv = reinterpret_cast<const V*>(p);
   const V* qv = reinterpret_cast<const V*>(q);
-  double a0 = 0.0, a1 = 0.0;
+  Acc<T> a0[W], a1[W];
+#pragma unroll
+  for (int k = 0; k < W; k++) a0[k] = a1[k] = Acc<T>(0);
   int64_t i = tid;
   for (; i + nthreads < nv; i += 2 * nthreads) {
     const V p0 = pv[i], q0 = qv[i], p1 = pv[i + nthreads], q1 = qv[i + nthreads];
 #pragma unroll
     for (int k = 0; k < W; k++) {
-      a0 += (double)vget<T>(p0, k) * (double)vget<T>(q0, k);
-      a1 += (double)vget<T>(p1, k) * (double)vget<T>(q1, k);
+      a0[k] += vget<T>(p0, k) * vget<T>(q0, k);
+      a1[k] += vget<T>(p1, k) * vget<T>(q1, k);
     }
   }
   for (; i < nv; i += nthreads) {
     const V p0 = pv[i], q0 = qv[i];
 #pragma unroll
-    for (int k = 0; k < W; k++) a0 += (double)vget<T>(p0, k) * (double)vget<T>(q0, k);
+    for (int k = 0; k < W; k++) a0[k] += vget<T>(p0, k) * vget<T>(q0, k);
   }
-  for (int64_t j = nv * W + tid; j < n; j += nthreads) a0 += (double)p[j] * (double)q[j];
-  return a0 + a1;
+  double tot = 0.0;
+#pragma unroll
+  for (int k = 0; k < W; k++) tot += (double)a0[k] + (double)a1[k];
+  for (int64_t j = nv * W + tid; j < n; j += nthreads) tot += (double)p[j] * (double)q[j];
+  return tot;
 }
 
-// x += a p; r -= a q; returns sum r.r (FP64 accumulation).
+// x += a p; r -= a q; returns sum r.r.
 template <typename T>
 __device__ __forceinline__ double vupdate(T* __restrict__ x, T* __restrict__ r,
                                           const T* __restrict__ p, const T* __restrict__ q,
@@ -151,7 +165,9 @@ __device__ __forceinline__ double vupdate(T* __restrict__ x, T* __restrict__ r,
   V* rv = reinterpret_cast<V*>(r);
   const V* pv = reinterpret_cast<const V*>(p);
   const V* qv = reinterpret_cast<const V*>(q);
-  double acc = 0.0;
+  Acc<T> acc[W];
+#pragma unroll
+  for (int k = 0; k < W; k++) acc[k] = Acc<T>(0);
   for (int64_t i = tid; i < nv; i += nthreads) {
     V xi = xv[i], ri = rv[i];
     const V pi = pv[i], qi = qv[i];
@@ -160,18 +176,21 @@ __device__ __forceinline__ double vupdate(T* __restrict__ x, T* __restrict__ r,
       vset<T>(xi, k, vget<T>(xi, k) + a * vget<T>(pi, k));
       const T rk = vget<T>(ri, k) - a * vget<T>(qi, k);
       vset<T>(ri, k, rk);
-      acc += (double)rk * (double)rk;
+      acc[k] += rk * rk;
     }
     xv[i] = xi;
     rv[i] = ri;
   }
+  double tot = 0.0;
+#pragma unroll
+  for (int k = 0; k < W; k++) tot += (double)acc[k];
   for (int64_t j = nv * W + tid; j < n; j += nthreads) {
     x[j] += a * p[j];
     const T rk = r[j] - a * q[j];
     r[j] = rk;
-    acc += (double)rk * (double)rk;
+    tot += (double)rk * (double)rk;
   }
-  return acc;
+  return tot;
 }
 
 // p = r + b p.
