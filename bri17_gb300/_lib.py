@@ -61,6 +61,9 @@ _SIGS = {
     "bri17_op_destroy": ([vp], ctypes.c_int),
     "bri17_op_info": ([vp, c_int64_p, c_int64_p], ctypes.c_int),
     "bri17_op_set_material": ([vp, ctypes.c_double, ctypes.c_double], ctypes.c_int),
+    "bri17_op_fused_form": ([vp, c_int_p], ctypes.c_int),
+    "bri17_op_set_fused_form": ([vp, ctypes.c_int], ctypes.c_int),
+    "bri17_wait_timeouts": ([c_int_p], ctypes.c_int),
     "bri17_op_set_pass_timing": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_op_pass_times": ([vp, c_double_p, c_int64_p, ctypes.c_int, c_int_p], ctypes.c_int),
     "bri17_pass_name": ([ctypes.c_int], ctypes.c_char_p),

@@ -131,6 +131,22 @@ class Hooke:
         return (f"Hooke<d,{self._grid.dim}>{{mu={_fmt(self._mu)},nu={_fmt(self._nu)},"
                 f"grid={self._grid!r}\n")
 
+    FUSED_FORMS = ("registers", "staged", "tma", "tma_registers")
+
+    @property
+    def fused_form(self) -> str:
+        """Form of the fused axis-0 pass (diagnostics): "registers",
+        "staged", "tma" or "tma_registers"; FP32 handles pick the fastest at
+        creation."""
+        f = ctypes.c_int()
+        check(_lib.load().bri17_op_fused_form(self._h, ctypes.byref(f)), "bri17_op_fused_form")
+        return self.FUSED_FORMS[f.value]
+
+    @fused_form.setter
+    def fused_form(self, form: str) -> None:
+        check(_lib.load().bri17_op_set_fused_form(self._h, self.FUSED_FORMS.index(form)),
+              "bri17_op_set_fused_form")
+
     def set_material(self, mu: float, nu: float) -> None:
         check(_lib.load().bri17_op_set_material(self._h, float(mu), float(nu)),
               "bri17_op_set_material")
@@ -278,6 +294,14 @@ class Hooke:
         if rc != 0 and raise_on_failure:
             check(rc, "bri17_cg_solve")
         return x, out
+
+
+def wait_timeouts() -> int:
+    """Bounded device waits that ran out on the current device since the
+    previous call (0 in normal operation)."""
+    n = ctypes.c_int()
+    check(_lib.load().bri17_wait_timeouts(ctypes.byref(n)), "bri17_wait_timeouts")
+    return n.value
 
 
 def version() -> str:

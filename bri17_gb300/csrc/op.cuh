@@ -31,7 +31,7 @@ struct bri17_op {
   bri17_op* twin32;    // FP32 twin of an FP64 handle for mixed-precision CG
   unsigned material_epoch;  // bumped by bri17_op_set_material
   void* timing;             // PassTiming while per-pass timing is enabled
-  int fused_form;           // axis-0 stiffness pass: 0 registers, 1 staged
+  int fused_form;           // axis-0 pass: 0 registers, 1 staged, 2 TMA, 3 TMA + registers
 };
 
 namespace bri17gb {

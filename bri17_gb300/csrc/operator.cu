@@ -5,9 +5,14 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
+
+#include <cudaTypedefs.h>
 
 #include "op.cuh"
 #include "passes.cuh"
@@ -244,9 +249,10 @@ static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
     const Plan8& p = g.p8_row;
     if (ct_rows_r2c<T>(p.n, x, X, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
-    const size_t smem = (3 * p.n + 1 + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
-    launch_pdl(rows_r2c_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st, 
-        x, X, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
+    const int pitch = exchange_pitch(p.n, rb, (int)sizeof(cplx<T>), false);
+    const size_t smem = (3 * p.n + 1 + (size_t)rb * pitch) * sizeof(cplx<T>);
+    launch_pdl(rows_r2c_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st,
+               x, X, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, pitch, mask);
     return BRI17_OK;
   }
   const int n = g.n[g.dim - 1];
@@ -268,9 +274,10 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
     const Plan8& p = g.p8_row;
     if (ct_rows_c2r<T>(p.n, X, x, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
     const int rb = rows_p8(p.T, nrows, mask.unit, mask.flags != nullptr);
-    const size_t smem = (2 * p.n + (size_t)rb * pitch8(p.n)) * sizeof(cplx<T>);
-    launch_pdl(rows_c2r_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st, 
-        X, x, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, mask);
+    const int pitch = exchange_pitch(p.n, rb, (int)sizeof(cplx<T>), false);
+    const size_t smem = (2 * p.n + (size_t)rb * pitch) * sizeof(cplx<T>);
+    launch_pdl(rows_c2r_p2<T, RtEng>, (unsigned)((nrows + rb - 1) / rb), p.T * rb, smem, st,
+               X, x, nrows, g.H, RtEng{p}, tab.tw[g.dim - 1], rb, pitch, mask);
     return BRI17_OK;
   }
   const int n = g.n[g.dim - 1];
@@ -284,6 +291,121 @@ static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
   return BRI17_OK;
 }
 
+namespace {
+
+// Wavefronts of one warp-wide shared-memory access: the largest number of
+// distinct 4-byte words any of the 32 banks serves.
+int access_wavefronts(const int* byte_addr, int lanes, int csize) {
+  int words[128];
+  int nw = 0;
+  for (int l = 0; l < lanes; l++)
+    for (int w = 0; w < csize / 4; w++) words[nw++] = byte_addr[l] / 4 + w;
+  int best = 0;
+  for (int b = 0; b < 32; b++) {
+    int distinct = 0;
+    for (int i = 0; i < nw; i++) {
+      if (words[i] % 32 != b) continue;
+      bool seen = false;
+      for (int k = 0; k < i && !seen; k++) seen = words[k] == words[i];
+      if (!seen) distinct++;
+    }
+    best = std::max(best, distinct);
+  }
+  return best;
+}
+
+long exchange_wavefronts(const Plan8& p, int lines, int pitch, int csize, bool lines_fastest) {
+  const int T = p.T;
+  const int nthreads = T * lines;
+  long total = 0;
+  int addr[32];
+  auto pad = [](int q) { return q + (q >> 4); };
+  for (int w0 = 0; w0 < nthreads; w0 += 32) {
+    const int lanes = std::min(32, nthreads - w0);
+    int Ns = 1;
+    for (int s = 0; s + 1 < p.nst; s++) {
+      const int R = p.radix[s], M = 8 / R;
+      for (int m = 0; m < M; m++)
+        for (int r = 0; r < R; r++) {
+          for (int l = 0; l < lanes; l++) {
+            const int tid = w0 + l;
+            const int line = lines_fastest ? tid % lines : tid / T;
+            const int t = lines_fastest ? tid / lines : tid % T;
+            const int j = t + T * m, jm = j & (Ns - 1);
+            addr[l] = (line * pitch + pad((j - jm) * R + jm + r * Ns)) * csize;
+          }
+          total += access_wavefronts(addr, lanes, csize);
+        }
+      for (int q = 0; q < 8; q++) {
+        for (int l = 0; l < lanes; l++) {
+          const int tid = w0 + l;
+          const int line = lines_fastest ? tid % lines : tid / T;
+          const int t = lines_fastest ? tid / lines : tid % T;
+          addr[l] = (line * pitch + pad(t + T * q)) * csize;
+        }
+        total += access_wavefronts(addr, lanes, csize);
+      }
+      Ns *= R;
+    }
+  }
+  return total;
+}
+
+}  // namespace
+
+int exchange_pitch(int n, int lines, int csize, bool lines_fastest) {
+  static std::mutex mu;
+  static std::map<long, int> cache;
+  const long key = (((long)n * 4096 + lines) * 64 + csize) * 2 + (lines_fastest ? 1 : 0);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  Plan8 p;
+  int best = pitch8(n);
+  if (make_plan8(n, &p) && lines >= 1) {
+    long best_w = -1;
+    for (int d = 0; d < 16; d++) {
+      const int pitch = n + n / 16 + d;
+      const long w = exchange_wavefronts(p, lines, pitch, csize, lines_fastest);
+      if (best_w < 0 || w < best_w) {
+        best_w = w;
+        best = pitch;
+      }
+    }
+  }
+  cache[key] = best;
+  return best;
+}
+
+bool encode_tiled_map_3d(CUtensorMap* map, const void* base, int elem_bytes, uint64_t dim0,
+                         uint64_t dim1, uint64_t dim2, uint64_t stride1_bytes,
+                         uint64_t stride2_bytes, uint32_t box0, uint32_t box1) {
+  // cuTensorMapEncodeTiled through the runtime's driver entry point (no
+  // link-time dependency on the driver library).
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      fn = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode || (elem_bytes != 4 && elem_bytes != 8)) return false;
+  const cuuint64_t dims[3] = {dim0, dim1, dim2};
+  const cuuint64_t strides[2] = {stride1_bytes, stride2_bytes};
+  const cuuint32_t box[3] = {box0, box1, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(
+      map, elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+      3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 template <typename T, bool INV>
 static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
                         const Tables<T>& tab, BatchMask mask, cudaStream_t st) {
@@ -291,10 +413,11 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
     const Plan8& p = g.p8[1];
     if (ct_axis_c2c<T, INV>(p.n, X, g.H, nouter, tab.tw[1], mask, st)) return BRI17_OK;
     const int TB = (int)std::min<int64_t>(kP2Threads / p.T, g.H);
-    const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
+    const int pitch = exchange_pitch(p.n, TB, (int)sizeof(cplx<T>), true);
+    const size_t smem = (p.n + (size_t)TB * pitch) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.H + TB - 1) / TB), (unsigned)nouter);
-    launch_pdl(axis_c2c_p2<T, INV, RtEng>, grid, p.T * TB, smem, st, X, g.H, TB, RtEng{p}, tab.tw[1],
-                                                             mask);
+    launch_pdl(axis_c2c_p2<T, INV, RtEng>, grid, p.T * TB, smem, st, X, g.H, TB, RtEng{p},
+               tab.tw[1], pitch, mask);
     return BRI17_OK;
   }
   const int n = g.n[1];
@@ -319,23 +442,35 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
   if (MODE == kModeStiffness && g.use_p8[0]) {
     const Plan8& p = g.p8[0];
     // Form chosen per handle (fused_form, autotuned at creation for FP32);
-    // BRI17_FUSED_FORM=registers|staged overrides it (for measurements).
+    // BRI17_FUSED_FORM=registers|staged|tma|tma_registers overrides it (for measurements).
+    // A form whose launcher declines the size falls through to the next.
     static const int env_form = [] {
       const char* e = getenv("BRI17_FUSED_FORM");
       if (!e) return -1;
-      return strcmp(e, "registers") == 0 ? 0 : strcmp(e, "staged") == 0 ? 1 : -1;
+      return strcmp(e, "registers") == 0       ? 0
+             : strcmp(e, "staged") == 0        ? 1
+             : strcmp(e, "tma") == 0           ? 2
+             : strcmp(e, "tma_registers") == 0 ? 3
+                                               : -1;
     }();
     const int form = env_form >= 0 ? env_form : fp.form;
+    if constexpr (std::is_same<T, float>::value && DIM == 3) {
+      if ((form == 2 || form == 3) &&
+          ct_axis0_stiffness_tma_f32(p.n, form == 3, X, g.P, g.cspec, bstride, batch, fp, mask,
+                                     st))
+        return BRI17_OK;
+    }
     if (form == 1 &&
         ct_axis0_stiffness_staged<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
       return BRI17_OK;
     if (ct_axis0_stiffness<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
       return BRI17_OK;
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / p.T, g.P));
-    const size_t smem = (p.n + (size_t)TB * pitch8(p.n)) * sizeof(cplx<T>);
+    const int pitch = exchange_pitch(p.n, TB, (int)sizeof(cplx<T>), true);
+    const size_t smem = (p.n + (size_t)TB * pitch) * sizeof(cplx<T>);
     dim3 grid((unsigned)((g.P + TB - 1) / TB), (unsigned)batch);
-    launch_pdl(axis0_stiffness_p2<T, DIM, RtEng>, grid, p.T * TB, smem, st, 
-        X, g.P, g.cspec, bstride, TB, RtEng{p}, fp, mask);
+    launch_pdl(axis0_stiffness_p2<T, DIM, RtEng>, grid, p.T * TB, smem, st,
+               X, g.P, g.cspec, bstride, TB, pitch, RtEng{p}, fp, mask);
     return BRI17_OK;
   }
   const int n0 = g.n[0];
@@ -566,10 +701,9 @@ int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
                                        (float*)b, batch, spec, nullptr, st);
 }
 
-// Times the two forms of the FP32 axis-0 stiffness pass on the handle's own
-// spectrum buffer (its contents are irrelevant to the timing) and keeps the
-// faster: the staged form wins where the register form's tile is too narrow
-// for full memory segments, the register form elsewhere.
+// Times the forms of the FP32 axis-0 stiffness pass (registers, staged,
+// TMA-staged with staged or register compute) on the handle's own spectrum buffer (its contents are
+// irrelevant to the timing) and keeps the fastest.
 void autotune_fused_form(bri17_op* op) {
   const Geometry& g = op->g;
   cudaStream_t st;
@@ -582,7 +716,7 @@ void autotune_fused_form(bri17_op* op) {
   cudaEventCreate(&e1);
   float best = 1e30f;
   int best_form = 0;
-  for (int form = 0; form < 2; form++) {
+  for (int form = 0; form < 4; form++) {
     op->fused_form = form;
     FusedParams<float> fp = fused_params<float>(op, op->tab32, kModeStiffness);
     BatchMask none;
@@ -1216,6 +1350,26 @@ extern "C" int bri17_eigenstress_rhs(bri17_op* op, const void* tau, void* b,
   int rc = ensure_spectrum(op, sym);
   if (rc != BRI17_OK) return rc;
   return eigenstress_rhs_batched_async(op, 1, tau, b, op->spec, (cudaStream_t)stream);
+}
+
+extern "C" int bri17_op_fused_form(const bri17_op* op, int* form) {
+  if (!op || !form) return invalid("null pointer");
+  *form = op->fused_form;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_op_set_fused_form(bri17_op* op, int form) {
+  if (!op) return invalid("null handle");
+  if (form < 0 || form > 3) return invalid("form must be 0, 1, 2 or 3");
+  op->fused_form = form;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_wait_timeouts(int* count) {
+  if (!count) return invalid("null pointer");
+  const cudaError_t e = tma_wait_timeouts_f32(count);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the wait-timeout count");
+  return BRI17_OK;
 }
 
 extern "C" int bri17_op_set_pass_timing(bri17_op* op, int enable) {

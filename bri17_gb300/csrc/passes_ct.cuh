@@ -42,9 +42,10 @@ bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx
     constexpr int E = CtE<T, N>::value;                                               \
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
-    const size_t smem = (3 * N + 1 + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);       \
+    const int pitch = exchange_pitch(N, rb, (int)sizeof(cplx<T>), false);             \
+    const size_t smem = (3 * N + 1 + (size_t)rb * pitch) * sizeof(cplx<T>);           \
     launch_pdl(rows_r2c_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
-        x, X, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
+        x, X, nrows, H, CtEng<N, E>{}, tw, rb, pitch, mask);                          \
     return true;                                                                      \
   }
     BRI17_CT_CASES(CASE)
@@ -64,9 +65,10 @@ bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx
     constexpr int E = CtE<T, N>::value;                                               \
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
-    const size_t smem = (2 * N + (size_t)rb * pitch8(N)) * sizeof(cplx<T>);           \
+    const int pitch = exchange_pitch(N, rb, (int)sizeof(cplx<T>), false);             \
+    const size_t smem = (2 * N + (size_t)rb * pitch) * sizeof(cplx<T>);               \
     launch_pdl(rows_c2r_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
-        X, x, nrows, H, CtEng<N, E>{}, tw, rb, mask);                                 \
+        X, x, nrows, H, CtEng<N, E>{}, tw, rb, pitch, mask);                          \
     return true;                                                                      \
   }
     BRI17_CT_CASES(CASE)
@@ -85,10 +87,11 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw
     constexpr int E = CtE<T, N>::value;                                                \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B));   \
-    const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
+    const int pitch = exchange_pitch(N, TB, (int)sizeof(cplx<T>), true);               \
+    const size_t smem = (N + (size_t)TB * pitch) * sizeof(cplx<T>);                    \
     dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);                        \
     launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E>>, grid, TT * TB, smem, st, X, B, TB, CtEng<N, E>{}, \
-                                                                  tw, mask);           \
+                                                                  tw, pitch, mask);    \
     return true;                                                                       \
   }
     BRI17_CT_CASES(CASE)
@@ -108,10 +111,11 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
     constexpr int E = kFusedE;                                                         \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / TT, P)); \
-    const size_t smem = (N + (size_t)TB * pitch8(N)) * sizeof(cplx<T>);                \
+    const int pitch = exchange_pitch(N, TB, (int)sizeof(cplx<T>), true);               \
+    const size_t smem = (N + (size_t)TB * pitch) * sizeof(cplx<T>);                    \
     dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
     launch_pdl(axis0_stiffness_p2<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,               \
-        X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                          \
+        X, P, cstride, bstride, TB, pitch, CtEng<N, E>{}, fp, mask);                   \
     return true;                                                                       \
   }
     BRI17_CT_CASES(CASE)
@@ -134,10 +138,11 @@ bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
     constexpr int E = 8;                                                               \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, P));   \
-    const size_t smem = (N + (size_t)TB * pitch8(N) + (size_t)DIM * TB * stash_pitch(N, TB, sizeof(cplx<T>))) * sizeof(cplx<T>);     \
+    const int pitch = exchange_pitch(N, TB, (int)sizeof(cplx<T>), true);               \
+    const size_t smem = (N + (size_t)TB * pitch + (size_t)DIM * TB * stash_pitch(N, TB, sizeof(cplx<T>))) * sizeof(cplx<T>);     \
     dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                         \
     launch_pdl(axis0_stiffness_staged<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,   \
-               X, P, cstride, bstride, TB, CtEng<N, E>{}, fp, mask);                   \
+               X, P, cstride, bstride, TB, pitch, CtEng<N, E>{}, fp, mask);            \
     return true;                                                                       \
   }
     BRI17_CT_CASES(CASE)

@@ -8,6 +8,7 @@
 #include "fft8_ct.cuh"
 #include "passes.cuh"
 #include "pdl.cuh"
+#include "tma.cuh"
 
 namespace bri17gb {
 
@@ -45,10 +46,9 @@ constexpr int kP2FusedThreads = 128;
 template <typename T, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     rows_r2c_p2(const T* __restrict__ x, cplx<T>* __restrict__ X, int64_t nrows, int H,
-                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
+                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, int pitch, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
-  const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* twh = tw + n;        // W_n^k / 2, k in [0, m]
   cplx<T>* bufs = twh + m + 1;
@@ -96,10 +96,9 @@ __global__ void __launch_bounds__(kP2Threads)
 template <typename T, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     rows_c2r_p2(const cplx<T>* __restrict__ X, T* __restrict__ x, int64_t nrows, int H,
-                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, BatchMask mask) {
+                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, int pitch, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
-  const int pitch = pitch8(m);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
   const int64_t row0 = (int64_t)blockIdx.x * RB;
@@ -139,10 +138,9 @@ __global__ void __launch_bounds__(kP2Threads)
 template <typename T, bool INV, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     axis_c2c_p2(cplx<T>* __restrict__ X, int64_t B, int TB, Eng p,
-                const cplx<T>* __restrict__ tw_g, BatchMask mask) {
+                const cplx<T>* __restrict__ tw_g, int pitch, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = p.n();
-  const int pitch = pitch8(n);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
@@ -231,11 +229,10 @@ __device__ __forceinline__ void stiffness_lf(T phi0, T chi0, T psi0, const LineF
 template <typename T, int DIM, class Eng>
 __global__ void __launch_bounds__(kP2FusedThreads)
     axis0_stiffness_p2(cplx<T>* __restrict__ X, int64_t P, int64_t cstride,
-                       int64_t bstride, int TB, Eng p0, FusedParams<T> fp,
+                       int64_t bstride, int TB, int pitch, Eng p0, FusedParams<T> fp,
                        BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = p0.n();
-  const int pitch = pitch8(n0);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n0;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
@@ -315,11 +312,10 @@ namespace bri17gb {
 template <typename T, int DIM, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     axis0_stiffness_staged(cplx<T>* __restrict__ X, int64_t P, int64_t cstride,
-                           int64_t bstride, int TB, Eng p0, FusedParams<T> fp,
+                           int64_t bstride, int TB, int pitch, Eng p0, FusedParams<T> fp,
                            BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n0 = p0.n();
-  const int pitch = pitch8(n0);
   // Staged lines are only read and written at a thread's own positions,
   // lanes stepping across the TB lines first: their pitch staggers lines by
   // 32 / TB elements modulo one 128-byte bank row.
@@ -396,6 +392,158 @@ __global__ void __launch_bounds__(kP2Threads)
   }
 }
 
+// Bounded mbarrier waits that ran out in this translation unit's TMA kernels.
+static __device__ int g_tma_timeouts;
+
+// Axis 0, fused stiffness, TMA-staged (3D): the CTA's tile -- TB consecutive
+// lines of all DIM components, n0 rows each, laid out [c][k0][line] in shared
+// memory -- arrives by tensor copies that one thread issues all at once (one
+// per component and 256 rows), so the whole tile's HBM traffic is in flight
+// together and no registers wait on it.  The transforms and K(k) u(k) run
+// between the tile and registers at each thread's own positions (as in the
+// staged form) and tensor copies write the tile back.  Lines past P read as
+// zeros and their stores are clipped by the copy engine.  The map views the
+// spectrum as [plane = batch entry * DIM + component][k0][2 P reals].
+//
+// KEEP selects where the spectra wait between the transforms: false parks
+// each component's forward transform in the tile (one component in
+// registers at a time); true keeps all DIM components in registers from the
+// forward transforms through K(k) u(k) to the inverse ones (fewer
+// shared-memory round trips, more registers).
+template <typename T, int DIM, class Eng, bool KEEP>
+__global__ void __launch_bounds__(256)
+    axis0_stiffness_tma(const __grid_constant__ CUtensorMap map, int64_t P, int TB, int pitch,
+                        Eng p0, FusedParams<T> fp, BatchMask mask) {
+  static_assert(DIM == 3, "three-dimensional grids only");
+  extern __shared__ __align__(128) unsigned char smem_tma[];
+  constexpr int kPer = (int)(sizeof(cplx<T>) / sizeof(T));  // map elements per complex
+  const int n0 = p0.n();
+  const int rows = n0 < 256 ? n0 : 256;  // box height (at most 256)
+  cplx<T>* tile = reinterpret_cast<cplx<T>*>(smem_tma);
+  cplx<T>* exch = tile + (size_t)DIM * n0 * TB;
+  cplx<T>* tw = exch + (size_t)TB * pitch;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + n0);
+  const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
+  const int64_t b = (int64_t)blockIdx.x * TB + tb;
+  const int x0 = (int)((int64_t)blockIdx.x * TB * kPer);
+  const int z = blockIdx.y;
+  pdl_launch_dependents();
+  if (threadIdx.x == 0) mbar_init(bar, 1);
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  pdl_wait();
+  if (mask.skip(blockIdx.y)) return;
+  // The copy destinations must be 128-byte aligned; the launch guarantees
+  // it, and a misplaced window skips the CTA with an error count.
+  if (smem_addr(tile) & 127u) {
+    if (threadIdx.x == 0) atomicAdd(&g_tma_timeouts, 1);
+    return;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(bar, (uint32_t)((size_t)DIM * n0 * TB * sizeof(cplx<T>)));
+    for (int c = 0; c < DIM; c++)
+      for (int r0 = 0; r0 < n0; r0 += rows)
+        tma_load_3d(tile + ((size_t)c * n0 + r0) * TB, &map, x0, r0, z * DIM + c, bar);
+  }
+  T s = fp.s, mu = fp.mu;
+  if (fp.mat) {
+    s = fp.mat[2 * blockIdx.y];
+    mu = fp.mat[2 * blockIdx.y + 1];
+  }
+  const bool valid = b < P;
+  int k1 = 0, k2 = 0;
+  if (valid) {
+    k1 = (int)(b / fp.H);
+    k2 = (int)(b - (int64_t)k1 * fp.H);
+  }
+  const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
+          psi1 = __ldg(fp.tab.kpsi[1] + k1);
+  const T phi2 = __ldg(fp.tab.kphi[2] + k2), chi2 = __ldg(fp.tab.kchi[2] + k2),
+          psi2 = __ldg(fp.tab.kpsi[2] + k2);
+  const LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
+  // One second of global time per wait; a wait that runs out is counted,
+  // the tile is neither transformed nor stored, and the CTA waits (bounded
+  // again) for its copies before leaving.
+  const bool arrived = mbar_wait(bar, 0, 1000000000ull);
+  if (__syncthreads_or(!arrived)) {
+    if (threadIdx.x == 0) {
+      atomicAdd(&g_tma_timeouts, 1);
+      mbar_wait(bar, 0, 1000000000ull);
+    }
+    return;
+  }
+  cplx<T>* buf = exch + tb * pitch;
+  if constexpr (KEEP) {
+    cplx<T> v[DIM][Eng::E];
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      const cplx<T>* tc = tile + (size_t)c * n0 * TB + tb;
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) v[c][q] = tc[(t + p0.T() * q) * TB];
+      p0.template run<T, false>(v[c], buf, t, tw, 1);
+    }
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++) {
+      const int k0 = t + p0.T() * q;
+      const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
+              psi0 = __ldg(fp.tab.kpsi[0] + k0);
+      cplx<T> u[DIM];
+#pragma unroll
+      for (int c = 0; c < DIM; c++) u[c] = v[c][q];
+      stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
+#pragma unroll
+      for (int c = 0; c < DIM; c++) v[c][q] = u[c];
+    }
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+      p0.template run<T, true>(v[c], buf, t, tw, 1);
+      cplx<T>* tc = tile + (size_t)c * n0 * TB + tb;
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[c][q];
+    }
+  } else {
+    cplx<T> v[Eng::E];
+#pragma unroll 1
+    for (int c = 0; c < DIM; c++) {
+      cplx<T>* tc = tile + (size_t)c * n0 * TB + tb;
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
+      p0.template run<T, false>(v, buf, t, tw, 1);
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
+    }
+#pragma unroll 2
+    for (int q = 0; q < Eng::E; q++) {
+      const int k0 = t + p0.T() * q;
+      const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
+              psi0 = __ldg(fp.tab.kpsi[0] + k0);
+      cplx<T> u[DIM];
+#pragma unroll
+      for (int c = 0; c < DIM; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
+      stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
+#pragma unroll
+      for (int c = 0; c < DIM; c++) tile[((size_t)c * n0 + k0) * TB + tb] = u[c];
+    }
+#pragma unroll 1
+    for (int c = 0; c < DIM; c++) {
+      cplx<T>* tc = tile + (size_t)c * n0 * TB + tb;
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
+      p0.template run<T, true>(v, buf, t, tw, 1);
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
+    }
+  }
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < DIM; c++)
+      for (int r0 = 0; r0 < n0; r0 += rows)
+        tma_store_3d(&map, x0, r0, z * DIM + c, tile + ((size_t)c * n0 + r0) * TB);
+    tma_store_commit_and_wait();
+  }
+}
+
 // Launchers of the compile-time-length kernels (passes_ct.cuh, instantiated
 // in passes_ct_f32.cu / passes_ct_f64.cu).  Each picks its own block
 // geometry and returns false, launching nothing, when the length has no
@@ -417,6 +565,12 @@ template <typename T, int DIM>
 bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
                                int64_t bstride, int batch, const FusedParams<T>& fp,
                                BatchMask mask, cudaStream_t st);
+// TMA-staged forms (FP32, 3D; `keep` as KEEP above); false when the layout
+// does not meet the tensor-copy alignment rules.
+bool ct_axis0_stiffness_tma_f32(int n0, bool keep, cplx<float>* X, int64_t P, int64_t cstride,
+                                int64_t bstride, int batch, const FusedParams<float>& fp,
+                                BatchMask mask, cudaStream_t st);
+void ct_set_smem_attrs_tma_f32(size_t max_smem);
 void ct_set_smem_attrs(size_t max_smem);
 
 }  // namespace bri17gb

@@ -117,6 +117,25 @@ const char* bri17_pass_name(int pass);
 int bri17_op_set_material(bri17_op* op, double mu, double nu);
 
 /*
+ * Form of the fused axis-0 stiffness pass (diagnostics; no reference
+ * counterpart): 0 register-resident, 1 shared-memory staged, 2 TMA-staged
+ * (tensor copies of whole tiles; FP32, 3D, even shape[1]), 3 TMA-staged with
+ * the spectra kept in registers between the transforms.  FP32 handles
+ * pick the fastest by timing at creation.  A form that does not apply to the
+ * handle's grid falls back to the next applicable one at launch.  Results
+ * agree between forms to rounding.
+ */
+int bri17_op_fused_form(const bri17_op* op, int* form);
+int bri17_op_set_fused_form(bri17_op* op, int form);
+
+/*
+ * Bounded device-side waits (tensor-copy completions) that ran out on the
+ * current device since the previous call; 0 in normal operation.  A nonzero
+ * count means some operator results of that period are invalid.
+ */
+int bri17_wait_timeouts(int* count);
+
+/*
  * Batched Hooke::modal_stiffness (include/bri17/bri17.hpp:247-292; exported
  * to Python as Hooke*f64.modal_stiffness_matrix, python/pybri17.cpp:82-87).
  * k_dev: n x dim int32 multi-indices; K_dev: n x dim x dim complex (row-major

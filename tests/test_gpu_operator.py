@@ -186,3 +186,56 @@ def test_pybri17_per_mode_methods(golden_modal):
         assert np.abs(B - c["B"][i]).max() <= 4e-15 * np.abs(c["B"]).max()
     with pytest.raises(ValueError):
         h.modal_stiffness_matrix(c["k"][0], np.zeros((3, 3), np.complex128))
+
+
+# Every form of the FP32 axis-0 stiffness pass against the oracle: register-
+# resident, shared-memory staged and TMA-staged (tensor copies of whole
+# tiles; 3D with an even shape[1]).  Shapes cover partial last tiles (P not a
+# multiple of the tile's lines), the 256-row box split (n0 = 512, 1024) and
+# one where the TMA form declines (odd shape[1]) and falls back.
+FORM_SHAPES = [
+    ((16, 8, 8), (1.0, 1.0, 1.0), 1.0, 0.3),
+    ((64, 10, 6), (1.0, 2.0, 0.5), 0.8, 0.2),
+    ((128, 16, 30), (1.0, 1.0, 1.0), 1.2, 0.35),
+    ((256, 12, 16), (1.0, 0.5, 0.5), 1.0, 0.3),
+    ((512, 8, 14), (2.0, 1.0, 1.0), 1.1, 0.4),
+    ((1024, 4, 8), (1.0, 1.0, 1.0), 0.9, 0.25),
+    ((64, 9, 8), (1.0, 1.0, 1.0), 1.0, 0.3),
+]
+
+
+@pytest.mark.parametrize("shape,L,mu,nu", FORM_SHAPES)
+def test_fused_forms_f32_match_oracle(shape, L, mu, nu):
+    import torch
+    from bri17_gb300 import wait_timeouts
+    h, ho = pair(shape, L, mu, nu, precision="f32")
+    assert h.fused_form in h.FUSED_FORMS
+    rng = np.random.default_rng(11)
+    u = mean_free_normal(rng, 3, shape).astype(np.float32)
+    f_ref = O.apply_stiffness(ho, u.astype(np.float64))
+    ud = to_dev(u)
+    assert wait_timeouts() >= 0
+    outs = {}
+    for form in h.FUSED_FORMS:
+        h.fused_form = form
+        outs[form] = h.apply_stiffness(ud)
+        torch.cuda.synchronize()
+        f = outs[form].cpu().numpy().astype(np.float64)
+        assert rel_l2(f, f_ref) <= TOL_F32, form
+    assert wait_timeouts() == 0
+    for form in ("staged", "tma", "tma_registers"):
+        d = float((outs[form] - outs["registers"]).norm() / outs["registers"].norm())
+        assert d <= 1e-6, form
+
+
+def test_tma_form_64_cubed():
+    """The TMA form at 64^3 (full tiles, one box per component)."""
+    from bri17_gb300 import wait_timeouts
+    shape = (64, 64, 64)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3, precision="f32")
+    h.fused_form = "tma"
+    rng = np.random.default_rng(12)
+    u = mean_free_normal(rng, 3, shape).astype(np.float32)
+    f = h.apply_stiffness(to_dev(u)).cpu().numpy().astype(np.float64)
+    assert rel_l2(f, O.apply_stiffness(ho, u.astype(np.float64))) <= TOL_F32
+    assert wait_timeouts() == 0
