@@ -352,7 +352,11 @@ def run_operator(args, precision="f64"):
                                      C.c_void_p(f_host.data_ptr()), sp)
     e2e_s = time.perf_counter() - t0
     e2e = {"value": dof * args.steps / e2e_s / 1e9, "unit": "GDoF/s",
-           "h2d_bytes_per_step": dof * scalar, "d2h_bytes_per_step": dof * scalar}
+           "h2d_bytes_per_step": dof * scalar, "d2h_bytes_per_step": dof * scalar,
+           "host_path": ("staged copies pipelined per component"
+                         if os.environ.get("BRI17_HOST_PATH") == "staged" else
+                         "page-locked buffers read and written in place by the first and "
+                         "last passes over the host link")}
     # Breakdown: the copies alone (same pinned buffers, one stream).
     dev = torch.empty_like(us[0])
     c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))

@@ -230,11 +230,30 @@ class Hooke:
             _stream_ptr(stream)), "bri17_apply_stiffness")
         return f
 
-    def apply_stiffness_host(self, u: np.ndarray) -> np.ndarray:
-        """f = K u with host arrays (copies in, applies, copies out)."""
+    def apply_stiffness_host(self, u):
+        """f = K u with host buffers: a numpy array (copied through device
+        staging buffers) or a CPU torch tensor; a page-locked tensor
+        (``tensor.pin_memory()``) is read in place by the first pass, and f
+        comes back page-locked and written in place by the last."""
+        n = self._grid.dim * self._grid.size
+        try:
+            torch = _torch()
+        except ImportError:
+            torch = None
+        if torch is not None and isinstance(u, torch.Tensor):
+            if u.is_cuda:
+                raise ValueError("apply_stiffness_host takes host buffers")
+            u = u.to(self.dtype).contiguous()
+            if u.numel() != n:
+                raise ValueError("wrong number of values")
+            f = torch.empty(u.shape, dtype=u.dtype, pin_memory=u.is_pinned())
+            check(_lib.load().bri17_apply_stiffness_host(
+                self._h, ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(f.data_ptr()),
+                _stream_ptr()), "bri17_apply_stiffness_host")
+            return f
         dt = np.float64 if self._precision == "f64" else np.float32
         u = np.ascontiguousarray(u, dtype=dt)
-        if u.size != self._grid.dim * self._grid.size:
+        if u.size != n:
             raise ValueError("wrong number of values")
         f = np.empty_like(u)
         check(_lib.load().bri17_apply_stiffness_host(

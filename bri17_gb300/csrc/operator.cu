@@ -1203,6 +1203,19 @@ extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
 // axis-0 pass needs all of the field at once.
 constexpr int kHostChunksPerComp = 1;  // finer chunks measured slower (launch tails)
 
+// Device address of a page-locked host buffer, or nullptr for memory the
+// runtime does not know as page-locked (pageable memory takes the copy
+// pipeline).
+static const void* device_view(const void* h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
 template <typename T>
 static int apply_host_pipelined(bri17_op* op, const T* u_host, T* f_host,
                                 cudaStream_t st) {
@@ -1314,6 +1327,28 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
   }
   int rc = ensure_spectrum(op, op->g.dim);
   if (rc != BRI17_OK) return rc;
+  // Page-locked host buffers are addressable from the GPU (over NVLink-C2C
+  // on Grace machines): the first pass then reads u and the last pass writes
+  // f in host memory directly, and the link traffic overlaps those passes'
+  // compute instead of running as separate copies before and after them.
+  // BRI17_HOST_PATH=staged forces the copy pipeline (for measurements).
+  static const bool force_staged = [] {
+    const char* e = getenv("BRI17_HOST_PATH");
+    return e && strcmp(e, "staged") == 0;
+  }();
+  const void* du = force_staged ? nullptr : device_view(u_host);
+  void* df = force_staged ? nullptr : const_cast<void*>(device_view(f_host));
+  if (du && df) {
+    if (op->precision == BRI17_F64)
+      rc = run_pipeline<double, kModeStiffness>(op, op->tab64, (const double*)du, (double*)df,
+                                                1, op->spec, nullptr, st);
+    else
+      rc = run_pipeline<float, kModeStiffness>(op, op->tab32, (const float*)du, (float*)df, 1,
+                                               op->spec, nullptr, st);
+    if (rc != BRI17_OK) return rc;
+    BRI17_CUDA_TRY(cudaStreamSynchronize(st));
+    return BRI17_OK;
+  }
   if (op->precision == BRI17_F64)
     return apply_host_pipelined<double>(op, (const double*)u_host, (double*)f_host, st);
   return apply_host_pipelined<float>(op, (const float*)u_host, (float*)f_host, st);

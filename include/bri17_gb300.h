@@ -201,8 +201,11 @@ int bri17_apply_stiffness_noalloc(int dim, const int* shape, const double* L,
                                   double* f_dev, void* stream);
 
 /*
- * Same operator with host buffers: copies u to the device, applies, copies f
- * back, and synchronises `stream`.  Pinned host memory gives full copy speed.
+ * Same operator with host buffers; synchronises `stream` before returning.
+ * Page-locked buffers (cudaHostAlloc / cudaHostRegister) are read and written
+ * in place by the first and last passes over the host link; other host
+ * memory goes through device staging buffers with the copies pipelined per
+ * component against the passes.
  */
 int bri17_apply_stiffness_host(bri17_op* op, const void* u_host, void* f_host,
                                void* stream);

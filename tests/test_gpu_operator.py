@@ -142,6 +142,31 @@ def test_host_buffer_entry_point():
     assert np.array_equal(f, h.apply_stiffness(to_dev(u)).cpu().numpy())
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_host_buffer_page_locked_in_place(precision):
+    """Page-locked host tensors: the passes read u and write f in host memory
+    (no staging copies); same values as the device entry point, bit for
+    bit, including in place (f aliasing u)."""
+    import torch
+    shape = (32, 24, 20)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3, precision=precision)
+    dt = torch.float64 if precision == "f64" else torch.float32
+    rng = np.random.default_rng(5)
+    u = torch.from_numpy(rng.standard_normal((3,) + shape)).to(dt).pin_memory()
+    f = h.apply_stiffness_host(u)
+    assert f.is_pinned() and not f.is_cuda
+    ref = h.apply_stiffness(u.cuda()).cpu()
+    assert torch.equal(f, ref)
+    tol = TOL_F64 if precision == "f64" else TOL_F32
+    assert rel_l2(f.double().numpy(), O.apply_stiffness(ho, u.double().numpy())) <= tol
+    import ctypes
+    from bri17_gb300 import _lib
+    w = u.clone().pin_memory()
+    assert _lib.load().bri17_apply_stiffness_host(
+        h.handle, ctypes.c_void_p(w.data_ptr()), ctypes.c_void_p(w.data_ptr()), None) == 0
+    assert torch.equal(w, ref)
+
+
 def test_modal_batch_matches_reference_fixture(golden_modal):
     """Batched Hooke::modal_stiffness equals the reference header's output
     bit for bit for in-range k; B and out-of-range K to 1e-15."""
