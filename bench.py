@@ -537,9 +537,6 @@ def make_tau(req):
 
 
 def run_serve(args):
-    import queue
-    import threading
-
     import torch
 
     from bri17_gb300 import CartesianGrid, Hooke
@@ -547,14 +544,13 @@ def run_serve(args):
     torch.cuda.set_device(0)
     nreq = args.requests
     reqs = serve_requests(nreq, 3)
-    # tau is generated ahead of arrival on a producer thread (numpy releases
-    # the GIL while filling); at most ~4 GB in flight.
-    q = queue.Queue(maxsize=48)
-
-    def producer():
-        for r in reqs:
-            q.put((r, make_tau(r)))
-    threading.Thread(target=producer, daemon=True).start()
+    # Every request's tau is generated before the timed region (16 GB of FP64
+    # for 512 requests; a generator thread alone produces them slower than
+    # the arrival rate, which would throttle the stream).  numpy releases the
+    # GIL while filling, so a thread pool spreads the work over the cores.
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        taus = list(ex.map(make_tau, reqs))
     srv = Server(memory_budget_bytes=args.memory_gb << 30, slots_per_bucket=args.slots)
     # Warm the buckets (graph capture, first-touch) with one tiny solve per size.
     for s in (32, 48, 64, 96, 128):
@@ -563,26 +559,27 @@ def run_serve(args):
     sampler = ClockSampler(0)
     sampler.start()
     t_start = srv.clock()
-    submitted, done, ready = 0, {}, None
+    submitted, done = 0, {}
     meta = {}
+    host_s = {"submit": 0.0, "step": 0.0, "steps": 0}
     while len(done) < nreq:
         now = srv.clock() - t_start
         while submitted < nreq:
-            if ready is None:
-                try:
-                    ready = q.get(timeout=0.0 if srv.pending else 0.05)
-                except Exception:
-                    break
-            r, tau = ready
+            r, tau = reqs[submitted], taus[submitted]
             if r["t"] > now:
                 break
             s = r["side"]
+            h0 = time.perf_counter()
             rid = srv.submit((s, s, s), (1, 1, 1), r["mu"], r["nu"], tau, tol=1e-8)
+            host_s["submit"] += time.perf_counter() - h0
             meta[rid] = r
+            taus[submitted] = None
             submitted += 1
-            ready = None
         if srv.pending:
+            h0 = time.perf_counter()
             srv.step()
+            host_s["step"] += time.perf_counter() - h0
+            host_s["steps"] += 1
             for res in srv.poll():
                 if res["id"] in meta:
                     done[res["id"]] = res
@@ -635,7 +632,12 @@ def run_serve(args):
         "batched_mixed": {"solves_per_s": nreq / makespan, "makespan_s": makespan,
                           "p50_latency_s": float(np.percentile(lat, 50)),
                           "p99_latency_s": float(np.percentile(lat, 99)),
-                          "succeeded": ok},
+                          "succeeded": ok,
+                          "p50_latency_s_per_size": {
+                              str(sz): float(np.percentile(
+                                  [lat[j] for j, i in enumerate(done) if meta[i]["side"] == sz],
+                                  50)) for sz in (32, 48, 64, 96, 128)},
+                          "host_time_s": host_s},
         "one_at_a_time_fp64": {"solves_per_s": nreq / base_makespan,
                                "makespan_s": base_makespan,
                                "p50_latency_s": float(np.percentile(lat_b, 50)),
@@ -663,7 +665,7 @@ def main():
                     help="operator workloads: grid other than 128x128x128 (e.g. 256x256x256)")
     ap.add_argument("--no-oracle", action="store_true")
     ap.add_argument("--requests", type=int, default=512)
-    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--slots", type=int, default=64)
     ap.add_argument("--memory-gb", type=int, default=48)
     ap.add_argument("--baseline-per-size", type=int, default=2)
     args = ap.parse_args()

@@ -12,8 +12,10 @@
 // iterations is replayed as a CUDA graph.  Converged or empty slots are
 // masked on the device (their CTAs exit at once), so requests that arrive
 // while others run are admitted into free slots without re-capturing.
-// Each bucket has its own stream; all buckets' graphs are launched before
-// any is waited on, so their work overlaps on the GPU.
+// Each bucket has its own stream and progresses on its own: a step retires
+// whichever chunks have completed and relaunches those buckets at once, so
+// buckets of different sizes overlap on the GPU and small ones are not held
+// to the pace of large ones.
 //
 // Per request (as bri17_cg_solve's mixed mode): b = RHS(tau), x = 0, one FP32
 // CG whose search direction is kept throughout; each time its recursive
@@ -27,6 +29,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <thread>
 #include <deque>
 #include <unordered_map>
 #include <vector>
@@ -52,11 +55,16 @@ struct Request {
   double t_submit = 0, t_admit = 0, t_finish = 0;
   int iters = 0, outer = 0, breakdowns = 0;
   double bb = 0, rel = 1, nr = 0;
+  double mat64[2] = {0, 0};  // upload sources (live until the copies ran)
+  float mat32[2] = {0, 0};
   int status = BRI17_OK;
   bool cancel = false;
 };
 
-enum SlotState { kFree = 0, kInner = 1 };
+// kInner: the slot's FP32 CG runs in the bucket's chunks.  kOuter: its FP64
+// outer residual has been enqueued; the decision (retire or restart) is
+// taken when the stream work that computes it has completed.
+enum SlotState { kFree = 0, kInner = 1, kOuter = 2 };
 
 struct Bucket {
   int shape[3];
@@ -78,7 +86,8 @@ struct Bucket {
   std::vector<int> slot_state;
   std::vector<Request*> slot_req;
   int64_t bytes = 0;
-  bool launched = false;
+  bool in_flight = false;  // work was enqueued on the stream and not yet retired
+  bool enqueued = false;   // work enqueued since the last launch decision
 };
 
 // --- batched CG kernels: grid (blocks, S), slot z = blockIdx.y -----------
@@ -310,7 +319,7 @@ using namespace bri17gb;
 
 struct bri17_server {
   int64_t budget = 0;
-  int max_active = 8;  // slots per bucket
+  int max_active = 8;  // most slots per bucket
   int64_t used = 0;
   int64_t next_id = 1;
   std::deque<Request*> queue;
@@ -332,6 +341,8 @@ namespace {
   } while (0)
 
 int64_t slot_bytes(int64_t n) { return n * (5 * 8 + 4 * 4); }
+
+constexpr int64_t kBucketDoF = 48ll << 20;
 
 int64_t bucket_bytes(const int* shape, int S) {
   int64_t size = (int64_t)shape[0] * shape[1] * shape[2];
@@ -388,8 +399,14 @@ int capture_graph(Bucket* B) {
 }
 
 int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
-  // The axis-1 pass launches S * 3 * n0 CTA rows (grid.y <= 65535).
-  const int S = std::max(1, std::min(srv->max_active, 65535 / (3 * q->shape[0])));
+  // Slots: enough for about kBucketDoF unknowns of batched work per
+  // iteration (at least 8; small geometries get many slots, so their
+  // requests are not queued behind a handful of slots), at most max_active;
+  // the axis-1 pass launches S * 3 * n0 CTA rows (grid.y <= 65535).
+  const int64_t n_slot = 3 * (int64_t)q->shape[0] * q->shape[1] * q->shape[2];
+  const int64_t want = std::max<int64_t>(8, (kBucketDoF + n_slot - 1) / n_slot);
+  const int S = (int)std::max<int64_t>(
+      1, std::min<int64_t>({(int64_t)srv->max_active, want, 65535 / (3 * q->shape[0])}));
   const int64_t bytes = bucket_bytes(q->shape, S);
   if (srv->used + bytes > srv->budget) return BRI17_ERR_BUSY;
   Bucket* B = new Bucket();
@@ -511,19 +528,26 @@ void finish(bri17_server* srv, Request* q, int status) {
   delete q;
 }
 
-// Admit q into slot z of B: upload tau and material, compute b, start the
-// outer loop (x = 0, r = b).
+// Admit q into slot z of B: upload tau and material, compute b, x = 0 and
+// the initial residual r = b, all enqueued on the bucket's stream; the first
+// outer decision (which starts the inner CG) is taken once it has run.
 int admit(bri17_server* srv, Bucket* B, int z, Request* q) {
   cudaStream_t s = B->stream;
   const int64_t n = B->n;
   q->t_admit = srv->now();
+  // The slot stays masked out of the chunks until its first outer decision.
+  ks_set_inactive<<<1, 1, 0, s>>>(B->st + z);
   SRV_TRY(cudaMemcpyAsync(B->tau, q->tau.data(), 6 * B->size * 8, cudaMemcpyHostToDevice, s));
   const double corr = B->op64->corr;
   const double scaling = q->mu / (1. - 2. * q->nu);
-  const double m64[2] = {scaling * corr, q->mu * corr};
-  const float m32[2] = {(float)m64[0], (float)m64[1]};
-  SRV_TRY(cudaMemcpyAsync(B->mat64 + 2 * z, m64, sizeof(m64), cudaMemcpyHostToDevice, s));
-  SRV_TRY(cudaMemcpyAsync(B->mat32 + 2 * z, m32, sizeof(m32), cudaMemcpyHostToDevice, s));
+  q->mat64[0] = scaling * corr;
+  q->mat64[1] = q->mu * corr;
+  q->mat32[0] = (float)q->mat64[0];
+  q->mat32[1] = (float)q->mat64[1];
+  SRV_TRY(cudaMemcpyAsync(B->mat64 + 2 * z, q->mat64, sizeof(q->mat64), cudaMemcpyHostToDevice,
+                          s));
+  SRV_TRY(cudaMemcpyAsync(B->mat32 + 2 * z, q->mat32, sizeof(q->mat32), cudaMemcpyHostToDevice,
+                          s));
   int rc = eigenstress_rhs_batched_async(B->op64, 1, B->tau, B->b + z * n, B->op64->spec, s);
   if (rc != BRI17_OK) return rc;
   SRV_TRY(cudaMemsetAsync(B->x + z * n, 0, n * 8, s));
@@ -532,10 +556,9 @@ int admit(bri17_server* srv, Bucket* B, int z, Request* q) {
   std::vector<double>().swap(q->tau);
   rc = enqueue_residual(B, z, true);
   if (rc != BRI17_OK) return rc;
-  SRV_TRY(cudaStreamSynchronize(s));
-  q->bb = B->st_host[z].aux;
-  B->slot_state[z] = kInner;
+  B->slot_state[z] = kOuter;
   B->slot_req[z] = q;
+  B->enqueued = true;
   return BRI17_OK;
 }
 
@@ -544,6 +567,7 @@ int admit(bri17_server* srv, Bucket* B, int z, Request* q) {
 int outer_decide(bri17_server* srv, Bucket* B, int z, bool* busy) {
   Request* q = B->slot_req[z];
   const double rr = B->st_host[z].aux;
+  if (q->outer == 0) q->bb = rr;  // the initial residual is b
   *busy = false;
   if (!isfinite(rr) || !isfinite(q->bb)) {
     q->rel = NAN;
@@ -576,6 +600,8 @@ int outer_decide(bri17_server* srv, Bucket* B, int z, bool* busy) {
         B->partials + z * kRedMaxBlocks, rr);
   }
   q->outer += 1;
+  B->slot_state[z] = kInner;
+  B->enqueued = true;
   *busy = true;
   return BRI17_OK;
 }
@@ -588,8 +614,8 @@ extern "C" int bri17_server_create(int64_t budget, int max_active, bri17_server*
     return BRI17_ERR_INVALID_ARGUMENT;
   }
   *out = nullptr;
-  if (budget <= 0 || max_active < 1 || max_active > 64) {
-    set_error("memory budget must be > 0 and max_active in [1, 64]");
+  if (budget <= 0 || max_active < 1 || max_active > 256) {
+    set_error("memory budget must be > 0 and max_active in [1, 256]");
     return BRI17_ERR_INVALID_ARGUMENT;
   }
   int ndev = 0;
@@ -680,13 +706,89 @@ extern "C" int bri17_server_cancel(bri17_server* srv, int64_t id) {
   return BRI17_OK;
 }
 
+namespace {
+
+// Retire side of one bucket whose enqueued work has completed.
+//  (a) Slots whose FP64 outer residual was enqueued: decide (retire the
+//      request, or restart its inner CG with a reliable update).
+//  (b) Slots whose inner CG stopped in the last chunk: x += d, enqueue the
+//      FP64 outer residual (decided at the next retire).
+// Nothing here waits for the stream, except the copy of a finished
+// request's solution to its host buffer.
+int retire(bri17_server* srv, Bucket* B) {
+  std::vector<int> outer_before, inner_before;
+  for (int z = 0; z < B->S; z++) {
+    if (B->slot_state[z] == kOuter) outer_before.push_back(z);
+    if (B->slot_state[z] == kInner) inner_before.push_back(z);
+  }
+  for (int z : outer_before) {
+    bool busy;
+    const int rc = outer_decide(srv, B, z, &busy);
+    if (rc != BRI17_OK) return rc;
+  }
+  for (int z : inner_before) {
+    Request* q = B->slot_req[z];
+    const CgState& h = B->st_host[z];
+    if (q->cancel && h.active) {
+      ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
+      B->enqueued = true;
+    }
+    if (!h.active || q->cancel) {
+      q->iters = h.iters;  // cumulative: reliable updates keep the count
+      q->breakdowns = h.flag != BRI17_OK ? q->breakdowns + 1 : 0;
+      if (q->breakdowns > 2) {
+        q->rel = NAN;
+        B->slot_state[z] = kFree;
+        B->slot_req[z] = nullptr;
+        finish(srv, q, BRI17_ERR_BREAKDOWN);
+        continue;
+      }
+      ks_axpy32<<<g1(B->n), 256, 0, B->stream>>>(B->x + z * B->n, B->d + z * B->n, 1.0, B->n);
+      const int rc = enqueue_residual(B, z, false);
+      if (rc != BRI17_OK) return rc;
+      B->slot_state[z] = kOuter;
+      B->enqueued = true;
+    } else if (h.iters >= q->max_iterations) {
+      ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
+      B->enqueued = true;
+    }
+  }
+  return BRI17_OK;
+}
+
+bool bucket_has_inner(const Bucket* B) {
+  for (int z = 0; z < B->S; z++)
+    if (B->slot_state[z] == kInner) return true;
+  return false;
+}
+
+}  // namespace
+
+// Buckets progress independently: a bucket's chunk (kSrvChunk CG
+// iterations of all its slots, one graph) is relaunched as soon as the
+// previous one has completed and been retired, so small geometries are not
+// held to the pace of large ones.  A step does not wait for chunks; when it
+// finds nothing to do it waits (bounded, about 0.2 ms) for any chunk to
+// complete before returning.
 extern "C" int bri17_server_step(bri17_server* srv, int* active) {
   if (!srv) {
     set_error("null pointer");
     return BRI17_ERR_INVALID_ARGUMENT;
   }
-  // 1. Admission: FIFO, skipping requests whose bucket is full (no
-  //    head-of-line blocking across geometries).
+  bool progress = false;
+  // 1. Retire completed chunks.
+  for (Bucket* B : srv->buckets) {
+    if (!B->in_flight) continue;
+    const cudaError_t qs = cudaStreamQuery(B->stream);
+    if (qs == cudaErrorNotReady) continue;
+    if (qs != cudaSuccess) return cuda_fail(qs, "server chunk");
+    B->in_flight = false;
+    progress = true;
+    const int rc = retire(srv, B);
+    if (rc != BRI17_OK) return rc;
+  }
+  // 2. Admission: FIFO, skipping requests whose bucket is full or has a
+  //    chunk in flight (no head-of-line blocking across geometries).
   for (auto it = srv->queue.begin(); it != srv->queue.end();) {
     Request* q = *it;
     Bucket* B = find_bucket(srv, q);
@@ -696,7 +798,7 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
         // Release an idle bucket of another geometry, then retry once.
         for (size_t i = 0; i < srv->buckets.size(); i++) {
           Bucket* E = srv->buckets[i];
-          bool idle = true;
+          bool idle = !E->in_flight;
           for (int z = 0; z < E->S; z++) idle = idle && E->slot_state[z] == kFree;
           if (idle) {
             srv->used -= E->bytes;
@@ -713,67 +815,44 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
       }
       if (rc != BRI17_OK) return rc;
     }
-    const int z = free_slot(B);
+    const int z = B->in_flight ? -1 : free_slot(B);
     if (z < 0) {
       ++it;
       continue;
     }
     it = srv->queue.erase(it);
-    int rc = admit(srv, B, z, q);
-    if (rc != BRI17_OK) return rc;
-    bool busy;
-    rc = outer_decide(srv, B, z, &busy);
+    progress = true;
+    const int rc = admit(srv, B, z, q);
     if (rc != BRI17_OK) return rc;
   }
-  // 2. One graph replay per bucket with work, all launched before any wait.
+  // 3. Every idle bucket: a chunk if some slot's inner CG runs; the bucket
+  //    stays in flight while any enqueued work (outer residuals,
+  //    admissions, restarts) has not been retired.
   for (Bucket* B : srv->buckets) {
-    B->launched = false;
-    for (int z = 0; z < B->S; z++)
-      if (B->slot_state[z] == kInner) B->launched = true;
-    if (B->launched) SRV_TRY(cudaGraphLaunch(B->graph, B->stream));
-  }
-  // 3. Outer steps of slots whose inner CG finished (or were cancelled).
-  for (Bucket* B : srv->buckets) {
-    if (!B->launched) continue;
-    SRV_TRY(cudaStreamSynchronize(B->stream));
-    std::vector<int> outer;
-    for (int z = 0; z < B->S; z++) {
-      if (B->slot_state[z] != kInner) continue;
-      Request* q = B->slot_req[z];
-      const CgState& h = B->st_host[z];
-      if (q->cancel && h.active) {
-        ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
-      }
-      if (!h.active || q->cancel) {
-        q->iters = h.iters;  // cumulative: reliable updates keep the count
-        q->breakdowns = h.flag != BRI17_OK ? q->breakdowns + 1 : 0;
-        if (q->breakdowns > 2) {
-          q->rel = NAN;
-          B->slot_state[z] = kFree;
-          B->slot_req[z] = nullptr;
-          finish(srv, q, BRI17_ERR_BREAKDOWN);
-          continue;
-        }
-        ks_axpy32<<<g1(B->n), 256, 0, B->stream>>>(B->x + z * B->n, B->d + z * B->n, 1.0,
-                                                   B->n);
-        int rc = enqueue_residual(B, z, false);
-        if (rc != BRI17_OK) return rc;
-        outer.push_back(z);
-      } else if (h.iters >= q->max_iterations) {
-        ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
-      }
+    if (B->in_flight) continue;
+    if (bucket_has_inner(B)) {
+      SRV_TRY(cudaGraphLaunch(B->graph, B->stream));
+      B->enqueued = true;
     }
-    if (outer.empty()) continue;
-    SRV_TRY(cudaStreamSynchronize(B->stream));
-    for (int z : outer) {
-      bool busy;
-      int rc = outer_decide(srv, B, z, &busy);
-      if (rc != BRI17_OK) return rc;
+    if (B->enqueued) {
+      B->in_flight = true;
+      B->enqueued = false;
+      progress = true;
+    }
+  }
+  // 4. Nothing to do: wait a little for a chunk to complete.
+  if (!progress) {
+    const auto t_end = std::chrono::steady_clock::now() + std::chrono::microseconds(200);
+    bool any = false;
+    while (!any && std::chrono::steady_clock::now() < t_end) {
+      for (Bucket* B : srv->buckets)
+        if (B->in_flight && cudaStreamQuery(B->stream) != cudaErrorNotReady) any = true;
+      if (!any) std::this_thread::sleep_for(std::chrono::microseconds(10));
     }
   }
   int n_active = 0;
   for (Bucket* B : srv->buckets)
-    for (int z = 0; z < B->S; z++) n_active += B->slot_state[z] == kInner;
+    for (int z = 0; z < B->S; z++) n_active += B->slot_state[z] != kFree;
   if (active) *active = n_active;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "server step");

@@ -19,7 +19,7 @@ from ._lib import check
 
 
 class Server:
-    def __init__(self, memory_budget_bytes: int = 8 << 30, slots_per_bucket: int = 8):
+    def __init__(self, memory_budget_bytes: int = 8 << 30, slots_per_bucket: int = 64):
         L = _lib.load()
         h = ctypes.c_void_p()
         check(L.bri17_server_create(int(memory_budget_bytes), int(slots_per_bucket),

@@ -278,6 +278,11 @@ typedef struct bri17_request_result {
   double finish_time_s;
 } bri17_request_result;
 
+/*
+ * max_active (1..256): most request slots per bucket (one bucket per grid
+ * geometry).  A bucket gets enough slots for about 48 M unknowns of batched
+ * work per iteration, at least 8, at most max_active.
+ */
 int bri17_server_create(int64_t memory_budget_bytes, int max_active,
                         bri17_server** srv);
 int bri17_server_destroy(bri17_server* srv);
