@@ -457,6 +457,14 @@ def oracle_solution(w, tau, threads):
     return O.eigenstress_solve(h, tau)
 
 
+def solve_reps(args, mode):
+    """Timed solves per mode of the CG workloads: --cg-reps when given, else
+    3 (mixed modes) and 1 (plain FP64, the slow one); median reported."""
+    if args.cg_reps:
+        return args.cg_reps
+    return 1 if mode == "plain" else 3
+
+
 def run_cg(args, w, tau_fn, label):
     import torch
 
@@ -478,7 +486,7 @@ def run_cg(args, w, tau_fn, label):
         hooke.cg_solve(b, tol=1e-2, mode=mode, raise_on_failure=False)
         torch.cuda.synchronize()
         times = []
-        for _ in range(max(1, args.steps)):
+        for _ in range(solve_reps(args, mode)):
             t0 = time.perf_counter()
             x, info = hooke.cg_solve(b, tol=1e-8, mode=mode, max_iterations=200000)
             torch.cuda.synchronize()
@@ -500,7 +508,7 @@ def run_cg(args, w, tau_fn, label):
         err["oracle_seconds"] = time.perf_counter() - t0
     line = {
         "metric": METRIC, "value": out["mixed"]["solves_per_s"], "unit": "solves/s",
-        "n_gpus": 1, "steps": max(1, args.steps), "warmup": 1, "higher_is_better": True,
+        "n_gpus": 1, "steps": solve_reps(args, "mixed"), "warmup": 1, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
         "data": "synthetic",
         "config": {"workload": label, "grid": list(shape), "dof": dof, "tol": 1e-8,
@@ -657,6 +665,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--cg-reps", type=int, default=0,
+                    help="timed solves per mode for --workload cg / aniso "
+                         "(default 3 mixed, 1 plain)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="operator",
                     choices=["operator", "operator_f32", "cg", "aniso", "serve"])
