@@ -254,6 +254,51 @@ def run_reference(args):
     return 0
 
 
+def float_pair_line(hooke, us, fs, nrot, args, dof, stream, u_host, f_host, hbm_peak):
+    """The same workload through the float-pair operator of the FP64 handle
+    (hi + lo floats on the FP32 pipe, FP64 fields in memory): device time
+    over K applications, end to end through the host entry point, and the
+    relative difference from the FP64 operator's output."""
+    import ctypes as C
+
+    import torch
+    from bri17_gb300 import _lib
+    L = _lib.load()
+    ref = hooke.apply_stiffness(us[0])
+    try:
+        hooke.set_float_pair(True)
+    except Exception:
+        return None
+    for i in range(args.warmup):
+        hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    diff = float((hooke.apply_stiffness(us[0]) - ref).norm() / ref.norm())
+    sp = C.c_void_p(stream.cuda_stream)
+    for _ in range(max(1, args.warmup)):
+        L.bri17_apply_stiffness_host(hooke.handle, C.c_void_p(u_host.data_ptr()),
+                                     C.c_void_p(f_host.data_ptr()), sp)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.bri17_apply_stiffness_host(hooke.handle, C.c_void_p(u_host.data_ptr()),
+                                     C.c_void_p(f_host.data_ptr()), sp)
+    e2e_s = time.perf_counter() - t0
+    form = hooke.fused_form
+    hooke.set_float_pair(False)
+    return {"value": dof / (ms * 1e-3) / 1e9, "unit": "GDoF/s", "ms_per_step": ms,
+            "dtype": "f32 pairs (48-bit significands), f64 fields",
+            "rel_diff_vs_f64_operator": diff,
+            "operator_hbm_frac": 16 * dof / (ms * 1e-3) / 1e9 / hbm_peak,
+            "e2e": {"value": dof * args.steps / e2e_s / 1e9, "unit": "GDoF/s"},
+            "axis0_form": form}
+
+
 def config_of(w, ngpus, precision="f64"):
     shape = w["shape"]
     return {"workload": f"operator f = K u, periodic grid "
@@ -396,6 +441,10 @@ def run_operator(args, precision="f64"):
                     "flops_per_launch": flops, "flop_model": "5 n log2 n per complex "
                     "transform + 56 per mode"}
         extra["operator_hbm_frac"] = 2 * dof * scalar / (ms_total / args.steps * 1e-3) / 1e9 / hbm_peak
+    if precision == "f64" and ws == 1:
+        fp = float_pair_line(hooke, us, fs, nrot, args, dof, stream, u_host, f_host, hbm_peak)
+        if fp is not None:
+            extra["f64_float_pair"] = fp
     line = {
         "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / max(1, args.steps),

@@ -147,6 +147,14 @@ class Hooke:
         check(_lib.load().bri17_op_set_fused_form(self._h, self.FUSED_FORMS.index(form)),
               "bri17_op_set_fused_form")
 
+    def set_float_pair(self, enable: bool) -> None:
+        """FP64 handles: apply_stiffness / apply_stiffness_host in float-pair
+        arithmetic (48-bit significands on the FP32 pipe; about 1e-14 from
+        the FP64 operator).  3D power-of-two grids, shape[0], shape[1] in
+        64..512 and shape[2] in 128..1024; raises Bri17Error otherwise."""
+        check(_lib.load().bri17_op_set_float_pair(self._h, 1 if enable else 0),
+              "bri17_op_set_float_pair")
+
     def set_material(self, mu: float, nu: float) -> None:
         check(_lib.load().bri17_op_set_material(self._h, float(mu), float(nu)),
               "bri17_op_set_material")

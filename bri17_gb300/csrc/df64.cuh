@@ -1,0 +1,169 @@
+// df64.cuh -- double-float ("float pair") arithmetic for the FP64-accurate
+// operator on the FP32 pipe.
+//
+// GB300 executes FP32 at about 60x its FP64 rate, while the FFT passes of the
+// FP64 operator are bound by the FP64 pipe.  A df64 value is the unevaluated
+// sum hi + lo of two floats with |lo| <= ulp(hi) / 2: 48 significant bits.
+// The operations are the classical error-free transformations (Knuth's
+// TwoSum, Dekker's FastTwoSum, the FMA-based exact product) combined as in
+// the double-double literature (Hida, Li & Bailey, "Library for double-double
+// and quad-double arithmetic", 2000; Joldes, Muller & Popescu, "Tight and
+// rigorous error bounds for basic building blocks of double-word
+// arithmetic", ACM TOMS 2017):
+//   add: |err| <= 2^-47 (|a| + |b|)  (the "sloppy" sum: the bound is relative
+//        to the operands, which is the bound the FFT error analysis uses);
+//   mul: |err| <= 2^-46 |a b|.
+// Every float operation is an explicitly rounded intrinsic (__fadd_rn,
+// __fmul_rn, __fmaf_rn), so the compiler can neither contract nor reorder
+// them.
+//
+// Exponent range: a value keeps its 48 bits while |lo| stays a normal float,
+// i.e. for |x| >= 2^-102 (about 2e-31); smaller parts of a field lose bits
+// gradually (norm-wise the error stays at the 2^-47 level of the field's
+// largest entries).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft.cuh"
+
+namespace bri17gb {
+
+struct __align__(8) df64 {
+  float hi, lo;
+  df64() = default;
+  // Exact split of a double into hi + lo (host, and compile-time constants
+  // in device code).
+  __host__ __device__ constexpr df64(double d)
+      : hi(static_cast<float>(d)),
+        lo(static_cast<float>(d - static_cast<double>(static_cast<float>(d)))) {}
+  __host__ __device__ constexpr df64(float h, float l) : hi(h), lo(l) {}
+};
+
+struct __align__(16) df64c {
+  df64 x, y;
+};
+
+template <>
+struct CplxOf<df64> {
+  using type = df64c;
+};
+
+__device__ __forceinline__ df64 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fadd_rn(s, -a);
+  const float e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
+  return df64(s, e);
+}
+
+// |a| >= |b| (or a == 0).
+__device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df64(s, __fadd_rn(b, -__fadd_rn(s, -a)));
+}
+
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const df64 s = df_two_sum(a.hi, b.hi);
+  const float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return df_fast_two_sum(s.hi, e);
+}
+
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+
+// a * b + c: df64, and the single-rounding FMA for float and double (these
+// overloads keep namespace-scope calls of fma(...) on the built-in FMA).
+__device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) { return a * b + c; }
+__device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// Loads of constant tables (read-only cache where the type allows).
+template <typename T>
+__device__ __forceinline__ T ldg_val(const T* p) {
+  return __ldg(p);
+}
+template <>
+__device__ __forceinline__ df64 ldg_val<df64>(const df64* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return df64(v.x, v.y);
+}
+
+// Real fields of a df64 operator are FP64 in memory.
+template <typename T>
+struct IoOf {
+  using type = T;
+};
+template <>
+struct IoOf<df64> {
+  using type = double;
+};
+
+template <typename T>
+__device__ __forceinline__ T from_io(typename IoOf<T>::type v) {
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ typename IoOf<T>::type to_io(T v) {
+  return v;
+}
+
+// double -> hi + lo without the FP64 pipe: the 53-bit significand is split
+// by integer operations into its top 24 bits rounded to nearest even (hi)
+// and the signed remainder (lo, rounded to 24 bits), each scaled by an
+// exact power of two.  Zeros and subnormal doubles give 0; infinities and
+// NaN give hi = the value converted to float, lo = 0.
+__device__ __forceinline__ float df_pow2(int e) {
+  // 2^e for e in [-149, 127] (subnormal range included), built exactly.
+  if (e >= -126) return __int_as_float((e + 127) << 23);
+  return __int_as_float(1 << (e + 149));
+}
+
+template <>
+__device__ __forceinline__ df64 from_io<df64>(double v) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  const bool neg = (bits >> 63) != 0;
+  if (ex == 0) return df64(0.f, 0.f);
+  if (ex == 0x7FF) return df64(__double2float_rn(v), 0.f);
+  const long long sig = (long long)((bits & ((1ull << 52) - 1)) | (1ull << 52));
+  long long q = sig >> 29;              // top 24 bits
+  long long r = sig & ((1ll << 29) - 1);  // low 29 bits
+  if (r > (1ll << 28) || (r == (1ll << 28) && (q & 1))) {
+    q += 1;
+    r -= 1ll << 29;
+  }
+  // value = sig * 2^(ex - 1075) = q * 2^(ex - 1046) + r * 2^(ex - 1075)
+  const int eh = ex - 1046, el = ex - 1075;
+  float hi, lo;
+  if (eh > 127 - 24) {
+    hi = __double2float_rn(v);  // beyond the float range: overflow as a float would
+    lo = 0.f;
+  } else {
+    // q <= 2^24 and |r| <= 2^28 convert to float (q exactly, r rounded);
+    // the power-of-two scalings are exact unless they underflow.
+    const float sh = eh >= -149 ? df_pow2(eh) : 0.f;
+    hi = __fmul_rn(__ll2float_rn(q), sh);
+    // Split the scaling of lo so that neither factor underflows early.
+    const int el1 = el < -126 ? -126 : el;
+    lo = __fmul_rn(__fmul_rn(__ll2float_rn(r), df_pow2(el1)),
+                   el < -126 ? (el - el1 >= -149 ? df_pow2(el - el1) : 0.f) : 1.f);
+  }
+  return neg ? df64(-hi, -lo) : df64(hi, lo);
+}
+
+template <>
+__device__ __forceinline__ double to_io<df64>(df64 v) {
+  return __dadd_rn((double)v.hi, (double)v.lo);
+}
+
+}  // namespace bri17gb

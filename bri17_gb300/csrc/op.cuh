@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "df64.cuh"
 
 struct bri17_op {
   bri17gb::Geometry g;
@@ -32,6 +33,12 @@ struct bri17_op {
   unsigned material_epoch;  // bumped by bri17_op_set_material
   void* timing;             // PassTiming while per-pass timing is enabled
   int fused_form;           // axis-0 pass: 0 registers, 1 staged, 2 TMA, 3 TMA + registers
+  // Float-pair arithmetic for bri17_apply_stiffness(_host) on FP64 handles
+  // (df64.cuh); tables built on first enable.
+  bool float_pair;
+  int fused_form_df;
+  void* table_df;
+  bri17gb::Tables<bri17gb::df64> tabdf;
 };
 
 namespace bri17gb {

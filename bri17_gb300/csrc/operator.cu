@@ -1098,6 +1098,7 @@ extern "C" int bri17_op_destroy(bri17_op* op) {
   cudaDeviceSynchronize();
   if (op->twin32) bri17_op_destroy(op->twin32);
   cudaFree(op->table_mem);
+  cudaFree(op->table_df);
   cudaFree(op->spec);
   cudaFree(op->stage_in);
   cudaFree(op->stage_out);
@@ -1184,6 +1185,164 @@ extern "C" int bri17_modal_eigenstress_to_opposite_strain_batch(
   return BRI17_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Float-pair (df64) stiffness operator on FP64 handles.
+
+// The five passes in float-pair arithmetic (3D, compile-time lengths
+// only).  `form` selects the axis-0 pass: 2 TMA-staged, else staged.
+static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
+                            cudaStream_t st) {
+  const Geometry& g = op->g;
+  const int dim = g.dim;
+  const Tables<df64>& tab = op->tabdf;
+  cplx<df64>* S = reinterpret_cast<cplx<df64>*>(op->spec);
+  BatchMask none;
+  none.flags = nullptr;
+  none.stride = 0;
+  none.unit = 1;
+  const int nl = g.n[dim - 1];
+  const int64_t rows = (int64_t)dim * (g.size / nl);
+  bool ok;
+  {
+    PassScope ps(op, 0, st);
+    ok = ct_rows_r2c<df64>(nl / 2, u, S, rows, g.H, tab.tw[dim - 1], none, st);
+  }
+  if (ok) {
+    PassScope ps(op, 1, st);
+    ok = ct_axis_c2c<df64, false>(g.n[1], S, g.H, (int64_t)dim * g.n[0], tab.tw[1], none, st);
+  }
+  if (ok) {
+    PassScope ps(op, 2, st);
+    FusedParams<df64> fp = fused_params<df64>(op, tab, kModeStiffness);
+    const int64_t bstride = (int64_t)dim * g.cspec;
+    bool done = false;
+    if (form == 2)
+      done = ct_axis0_stiffness_tma_df(g.n[0], S, g.P, g.cspec, bstride, 1, fp, none, st);
+    if (!done)
+      done = ct_axis0_stiffness_staged<df64, 3>(g.n[0], S, g.P, g.cspec, bstride, 1, fp, none,
+                                                st);
+    ok = done;
+  }
+  if (ok) {
+    PassScope ps(op, 3, st);
+    ok = ct_axis_c2c<df64, true>(g.n[1], S, g.H, (int64_t)dim * g.n[0], tab.tw[1], none, st);
+  }
+  if (ok) {
+    PassScope ps(op, 4, st);
+    ok = ct_rows_c2r<df64>(nl / 2, S, f, rows, g.H, tab.tw[dim - 1], none, st);
+  }
+  if (!ok) {
+    set_error("float-pair operator: no compiled instance for this grid");
+    return BRI17_ERR_UNSUPPORTED_SIZE;
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "float-pair operator launch");
+  return BRI17_OK;
+}
+
+// Whether every pass of the grid has a compile-time float-pair instance:
+// 3D, power-of-two axes, shape[0] and shape[1] in 64..512, shape[2] in
+// 128..1024.
+static bool float_pair_supported(const Geometry& g) {
+  if (g.dim != 3) return false;
+  for (int i = 0; i < 2; i++)
+    if (!is_pow2(g.n[i]) || g.n[i] < 64 || g.n[i] > 512) return false;
+  return is_pow2(g.n[2]) && g.n[2] >= 128 && g.n[2] <= 1024;
+}
+
+// Times the axis-0 forms of the float-pair operator on the handle's own
+// buffers and keeps the fastest (as autotune_fused_form does for FP32).
+static void autotune_df_form(bri17_op* op) {
+  cudaStream_t st;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  void* u = nullptr;
+  const size_t bytes = (size_t)op->g.dim * op->g.size * sizeof(double);
+  if (cudaMalloc(&u, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamDestroy(st);
+    return;
+  }
+  cudaMemsetAsync(u, 0, bytes, st);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int best_form = 1;
+  for (int form = 1; form <= 2; form++) {
+    float ms = 0.f;
+    bool ok = true;
+    for (int rep = 0; rep < 3 && ok; rep++) {
+      cudaEventRecord(e0, st);
+      ok = run_stiffness_df(op, (const double*)u, (double*)u, form, st) == BRI17_OK;
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0) ms += t;
+    }
+    if (ok && ms < best) {
+      best = ms;
+      best_form = form;
+    }
+  }
+  op->fused_form_df = best_form;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(u);
+  cudaStreamDestroy(st);
+  cudaGetLastError();
+}
+
+extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
+  if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
+  if (!enable) {
+    op->float_pair = false;
+    return BRI17_OK;
+  }
+  if (op->precision != BRI17_F64) return invalid("float-pair arithmetic needs an FP64 handle");
+  if (!float_pair_supported(op->g)) {
+    set_error("float-pair operator: 3D power-of-two grids, shape[0], shape[1] in 64..512, "
+              "shape[2] in 128..1024");
+    return BRI17_ERR_UNSUPPORTED_SIZE;
+  }
+  if (!op->table_df) {
+    const Geometry& g = op->g;
+    std::vector<HostTables> ht(g.dim);
+    for (int i = 0; i < g.dim; i++) host_tables(g.n[i], op->L[i], &ht[i]);
+    const size_t b = tables_bytes(g.n, g.dim, sizeof(df64));
+    std::vector<unsigned char> host(b + 16);
+    void* mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, b + 16);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(float-pair tables)");
+    size_t off = 0;
+    fill_tables<df64>(ht, g.n, g.dim, host.data(), &off, &op->tabdf, (unsigned char*)mem);
+    e = cudaMemcpy(mem, host.data(), off, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(mem);
+      return cuda_fail(e, "cudaMemcpy(float-pair tables)");
+    }
+    op->table_df = mem;
+    static std::once_flag once;
+    std::call_once(once, [] {
+      ct_set_smem_attrs_df_rows(kMaxSmem);
+      ct_set_smem_attrs_df_c2c(kMaxSmem);
+      ct_set_smem_attrs_df_axis0(kMaxSmem);
+    });
+    const int rc = ensure_spectrum(op, op->g.dim);
+    if (rc != BRI17_OK) return rc;
+    autotune_df_form(op);
+  }
+  op->float_pair = true;
+  return BRI17_OK;
+}
+
 extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
                                      void* stream) {
   if (!op) return invalid("null handle");
@@ -1192,6 +1351,12 @@ extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
     if (dc != BRI17_OK) return dc;
   }
   if (!u || !f) return invalid("null pointer");
+  if (op->float_pair) {
+    const int rc = ensure_spectrum(op, op->g.dim);
+    if (rc != BRI17_OK) return rc;
+    return run_stiffness_df(op, (const double*)u, (double*)f, op->fused_form_df,
+                            (cudaStream_t)stream);
+  }
   return apply_stiffness_async(op, u, f, (cudaStream_t)stream);
 }
 
@@ -1339,13 +1504,26 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
   const void* du = force_staged ? nullptr : device_view(u_host);
   void* df = force_staged ? nullptr : const_cast<void*>(device_view(f_host));
   if (du && df) {
-    if (op->precision == BRI17_F64)
+    if (op->float_pair)
+      rc = run_stiffness_df(op, (const double*)du, (double*)df, op->fused_form_df, st);
+    else if (op->precision == BRI17_F64)
       rc = run_pipeline<double, kModeStiffness>(op, op->tab64, (const double*)du, (double*)df,
                                                 1, op->spec, nullptr, st);
     else
       rc = run_pipeline<float, kModeStiffness>(op, op->tab32, (const float*)du, (float*)df, 1,
                                                op->spec, nullptr, st);
     if (rc != BRI17_OK) return rc;
+    BRI17_CUDA_TRY(cudaStreamSynchronize(st));
+    return BRI17_OK;
+  }
+  if (op->float_pair) {
+    // Pageable buffers: whole-field copies around the float-pair passes.
+    const size_t bytes = (size_t)op->g.dim * op->g.size * sizeof(double);
+    BRI17_CUDA_TRY(cudaMemcpyAsync(op->stage_in, u_host, bytes, cudaMemcpyHostToDevice, st));
+    rc = run_stiffness_df(op, (const double*)op->stage_in, (double*)op->stage_out,
+                          op->fused_form_df, st);
+    if (rc != BRI17_OK) return rc;
+    BRI17_CUDA_TRY(cudaMemcpyAsync(f_host, op->stage_out, bytes, cudaMemcpyDeviceToHost, st));
     BRI17_CUDA_TRY(cudaStreamSynchronize(st));
     return BRI17_OK;
   }
@@ -1389,21 +1567,27 @@ extern "C" int bri17_eigenstress_rhs(bri17_op* op, const void* tau, void* b,
 
 extern "C" int bri17_op_fused_form(const bri17_op* op, int* form) {
   if (!op || !form) return invalid("null pointer");
-  *form = op->fused_form;
+  *form = op->float_pair ? op->fused_form_df : op->fused_form;
   return BRI17_OK;
 }
 
 extern "C" int bri17_op_set_fused_form(bri17_op* op, int form) {
   if (!op) return invalid("null handle");
   if (form < 0 || form > 3) return invalid("form must be 0, 1, 2 or 3");
-  op->fused_form = form;
+  if (op->float_pair)
+    op->fused_form_df = form == 2 ? 2 : 1;  // float pairs: staged or TMA-staged
+  else
+    op->fused_form = form;
   return BRI17_OK;
 }
 
 extern "C" int bri17_wait_timeouts(int* count) {
   if (!count) return invalid("null pointer");
-  const cudaError_t e = tma_wait_timeouts_f32(count);
+  int a = 0, b = 0;
+  cudaError_t e = tma_wait_timeouts_f32(&a);
+  if (e == cudaSuccess) e = tma_wait_timeouts_df(&b);
   if (e != cudaSuccess) return cuda_fail(e, "reading the wait-timeout count");
+  *count = a + b;
   return BRI17_OK;
 }
 

@@ -6,12 +6,21 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "passes_p2.cuh"
 
 namespace bri17gb {
 
 #define BRI17_CT_CASES(X) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
+
+// Lengths with compile-time instances per scalar type: every case of
+// BRI17_CT_CASES for FP32 and FP64; 64..512 for float pairs (their kernels
+// are long to compile, and the grids that use them are 64..1024 per axis).
+template <typename T>
+constexpr bool ct_has(int n) {
+  return std::is_same<T, df64>::value ? (n >= 64 && n <= 512) : true;
+}
 
 // Elements per thread for scalar T and line length N (single-component
 // passes); the fused axis-0 pass holds DIM components per thread and uses 8.
@@ -33,11 +42,14 @@ inline int ct_rows_per_cta(int T, int64_t nrows, const BatchMask& mask) {
 }
 
 template <typename T>
-bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx<T>* tw,
-                 BatchMask mask, cudaStream_t st) {
+bool ct_rows_r2c(int m, const typename IoOf<T>::type* x, cplx<T>* X, int64_t nrows, int H,
+                 const cplx<T>* tw, BatchMask mask, cudaStream_t st) {
   switch (m) {
 #define CASE(N)                                                                       \
   case N: {                                                                           \
+    if constexpr (!ct_has<T>(N)) {                                                    \
+      return false;                                                                   \
+    } else {                                                                          \
     if (N > 512) return false;                                                        \
     constexpr int E = CtE<T, N>::value;                                               \
     const int TT = N / E;                                                             \
@@ -47,6 +59,7 @@ bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx
     launch_pdl(rows_r2c_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         x, X, nrows, H, CtEng<N, E>{}, tw, rb, pitch, mask);                          \
     return true;                                                                      \
+    }                                                                                 \
   }
     BRI17_CT_CASES(CASE)
 #undef CASE
@@ -56,11 +69,14 @@ bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx
 }
 
 template <typename T>
-bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx<T>* tw,
-                 BatchMask mask, cudaStream_t st) {
+bool ct_rows_c2r(int m, const cplx<T>* X, typename IoOf<T>::type* x, int64_t nrows, int H,
+                 const cplx<T>* tw, BatchMask mask, cudaStream_t st) {
   switch (m) {
 #define CASE(N)                                                                       \
   case N: {                                                                           \
+    if constexpr (!ct_has<T>(N)) {                                                    \
+      return false;                                                                   \
+    } else {                                                                          \
     if (N > 512) return false;                                                        \
     constexpr int E = CtE<T, N>::value;                                               \
     const int TT = N / E;                                                             \
@@ -70,6 +86,7 @@ bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx
     launch_pdl(rows_c2r_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         X, x, nrows, H, CtEng<N, E>{}, tw, rb, pitch, mask);                          \
     return true;                                                                      \
+    }                                                                                 \
   }
     BRI17_CT_CASES(CASE)
 #undef CASE
@@ -83,7 +100,10 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw
                  BatchMask mask, cudaStream_t st) {
   switch (n) {
 #define CASE(N)                                                                        \
-  case N: {                                                                            \
+  case N: {                                                                           \
+    if constexpr (!ct_has<T>(N)) {                                                    \
+      return false;                                                                   \
+    } else {                                                                          \
     constexpr int E = CtE<T, N>::value;                                                \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B));   \
@@ -93,6 +113,7 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw
     launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E>>, grid, TT * TB, smem, st, X, B, TB, CtEng<N, E>{}, \
                                                                   tw, pitch, mask);    \
     return true;                                                                       \
+    }                                                                                 \
   }
     BRI17_CT_CASES(CASE)
 #undef CASE
@@ -107,7 +128,10 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
                         cudaStream_t st) {
   switch (n0) {
 #define CASE(N)                                                                        \
-  case N: {                                                                            \
+  case N: {                                                                           \
+    if constexpr (!ct_has<T>(N)) {                                                    \
+      return false;                                                                   \
+    } else {                                                                          \
     constexpr int E = kFusedE;                                                         \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2FusedThreads / TT, P)); \
@@ -117,6 +141,7 @@ bool ct_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t 
     launch_pdl(axis0_stiffness_p2<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,               \
         X, P, cstride, bstride, TB, pitch, CtEng<N, E>{}, fp, mask);                   \
     return true;                                                                       \
+    }                                                                                 \
   }
     BRI17_CT_CASES(CASE)
 #undef CASE
@@ -134,7 +159,10 @@ bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
                                BatchMask mask, cudaStream_t st) {
   switch (n0) {
 #define CASE(N)                                                                        \
-  case N: {                                                                            \
+  case N: {                                                                           \
+    if constexpr (!ct_has<T>(N)) {                                                    \
+      return false;                                                                   \
+    } else {                                                                          \
     constexpr int E = 8;                                                               \
     const int TT = N / E;                                                              \
     const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, P));   \
@@ -144,12 +172,107 @@ bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
     launch_pdl(axis0_stiffness_staged<T, DIM, CtEng<N, E>>, grid, TT * TB, smem, st,   \
                X, P, cstride, bstride, TB, pitch, CtEng<N, E>{}, fp, mask);            \
     return true;                                                                       \
+    }                                                                                 \
   }
     BRI17_CT_CASES(CASE)
 #undef CASE
     default:
       return false;
   }
+}
+
+// TMA-staged form (3D): lines per CTA give tile rows of 128 bytes up to
+// n0 = 128, 64 bytes at 256 and 32 bytes from 512, with at most 256 threads
+// and at least two lines (the copies' x offsets stay 16-byte multiples).
+template <typename T>
+constexpr int tma_lines(int n0) {
+  const int bytes = n0 <= 128 ? 128 : n0 <= 256 ? 64 : 32;
+  const int cap = 256 / (n0 / 8 > 0 ? n0 / 8 : 1);
+  const int tb = bytes / (int)sizeof(cplx<T>) < cap ? bytes / (int)sizeof(cplx<T>) : cap;
+  return tb < 2 ? 2 : tb;
+}
+
+template <typename T, int N>
+int tma_pitch() {
+  return exchange_pitch(N, tma_lines<T>(N), (int)sizeof(cplx<T>), true);
+}
+
+template <typename T, int N>
+size_t tma_smem_bytes() {
+  constexpr int TB = tma_lines<T>(N);
+  return ((size_t)3 * N * TB + (size_t)TB * tma_pitch<T, N>() + N) * sizeof(cplx<T>) + 16;
+}
+
+// WITH_KEEP = false compiles only the staged-compute variant (keep is then
+// ignored).
+template <typename T, bool WITH_KEEP = true>
+bool ct_axis0_stiffness_tma(int n0, bool keep, cplx<T>* X, int64_t P, int64_t cstride,
+                            int64_t bstride, int batch, const FusedParams<T>& fp,
+                            BatchMask mask, cudaStream_t st) {
+  constexpr int DIM = 3;
+  constexpr int kPer = (int)(sizeof(cplx<T>) / sizeof(T));
+  // The map's strides (P and cstride complex) must be multiples of 16
+  // bytes, the base 16-byte aligned, and the planes evenly spaced.
+  if ((P * (int64_t)sizeof(cplx<T>)) % 16 != 0 || cstride != (int64_t)n0 * P ||
+      bstride != DIM * cstride)
+    return false;
+  if (reinterpret_cast<uintptr_t>(X) % 16 != 0) return false;
+  if ((int64_t)P * kPer >= ((int64_t)1 << 31)) return false;
+  switch (n0) {
+#define CASE(N)                                                                          \
+  case N: {                                                                           \
+    if constexpr (!ct_has<T>(N)) {                                                    \
+      return false;                                                                   \
+    } else {                                                                          \
+    constexpr int E = 8;                                                                 \
+    constexpr int TT = N / E;                                                            \
+    constexpr int TB = tma_lines<T>(N);                                                  \
+    static_assert(TT * TB <= 256 && TB % 2 == 0, "tile shape");                          \
+    const int rows = N < 256 ? N : 256;                                                  \
+    CUtensorMap map;                                                                     \
+    if (!encode_tiled_map_3d(&map, X, (int)sizeof(T), (uint64_t)P * kPer, N,             \
+                             (uint64_t)DIM * batch, (uint64_t)P * sizeof(cplx<T>),       \
+                             (uint64_t)cstride * sizeof(cplx<T>), kPer * TB, rows))      \
+      return false;                                                                      \
+    dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                           \
+    bool launched = false;                                                               \
+    if constexpr (WITH_KEEP) {                                                           \
+      if (keep) {                                                                        \
+        launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, true>, grid, TT * TB,        \
+                   tma_smem_bytes<T, N>(), st, map, P, TB, tma_pitch<T, N>(),            \
+                   CtEng<N, E>{}, fp, mask);                                             \
+        launched = true;                                                                 \
+      }                                                                                  \
+    }                                                                                    \
+    if (!launched)                                                                       \
+      launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, false>, grid, TT * TB,         \
+                 tma_smem_bytes<T, N>(), st, map, P, TB, tma_pitch<T, N>(), CtEng<N, E>{}, \
+                 fp, mask);                                                              \
+    return true;                                                                         \
+    }                                                                                 \
+  }
+    CASE(16) CASE(32) CASE(64) CASE(128) CASE(256) CASE(512) CASE(1024)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+template <typename T, bool WITH_KEEP = true>
+void ct_set_smem_attrs_tma(size_t max_smem) {
+#define CASE(N)                                                                          \
+  if constexpr (ct_has<T>(N)) {                                                          \
+    cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, false>,                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,                    \
+                         (int)std::min(max_smem, tma_smem_bytes<T, N>()));               \
+    if constexpr (WITH_KEEP)                                                             \
+      cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, true>,                 \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,                  \
+                           (int)std::min(max_smem, tma_smem_bytes<T, N>()));             \
+  }
+  CASE(16) CASE(32) CASE(64) CASE(128) CASE(256) CASE(512) CASE(1024)
+#undef CASE
+  cudaGetLastError();
 }
 
 template <typename T>
@@ -180,10 +303,10 @@ void ct_set_smem_attrs_t(size_t max_smem) {
 }
 
 #define BRI17_CT_INSTANTIATE(T)                                                             \
-  template bool ct_rows_r2c<T>(int, const T*, cplx<T>*, int64_t, int, const cplx<T>*,      \
-                               BatchMask, cudaStream_t);                                   \
-  template bool ct_rows_c2r<T>(int, const cplx<T>*, T*, int64_t, int, const cplx<T>*,      \
-                               BatchMask, cudaStream_t);                                   \
+  template bool ct_rows_r2c<T>(int, const typename IoOf<T>::type*, cplx<T>*, int64_t, int,  \
+                               const cplx<T>*, BatchMask, cudaStream_t);                   \
+  template bool ct_rows_c2r<T>(int, const cplx<T>*, typename IoOf<T>::type*, int64_t, int,  \
+                               const cplx<T>*, BatchMask, cudaStream_t);                   \
   template bool ct_axis_c2c<T, false>(int, cplx<T>*, int64_t, int64_t, const cplx<T>*,      \
                                       BatchMask, cudaStream_t);                             \
   template bool ct_axis_c2c<T, true>(int, cplx<T>*, int64_t, int64_t, const cplx<T>*,       \

@@ -4,6 +4,7 @@
 // serving every other length.
 #pragma once
 
+#include "df64.cuh"
 #include "fft8.cuh"
 #include "fft8_ct.cuh"
 #include "passes.cuh"
@@ -45,8 +46,10 @@ constexpr int kP2FusedThreads = 128;
 // n/2+1 complex.  T = m/8 threads per row, RB rows per CTA.
 template <typename T, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
-    rows_r2c_p2(const T* __restrict__ x, cplx<T>* __restrict__ X, int64_t nrows, int H,
-                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, int pitch, BatchMask mask) {
+    rows_r2c_p2(const typename IoOf<T>::type* __restrict__ x, cplx<T>* __restrict__ X,
+                int64_t nrows, int H, Eng pm, const cplx<T>* __restrict__ tw_g, int RB,
+                int pitch, BatchMask mask) {
+  using Io = typename IoOf<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -65,9 +68,16 @@ __global__ void __launch_bounds__(kP2Threads)
   pdl_wait();
   if (mask.skip(row0)) return;
   cplx<T> v[Eng::E];
-  const cplx<T>* xc = reinterpret_cast<const cplx<T>*>(x) + row * m;
+  const cplx<Io>* xc = reinterpret_cast<const cplx<Io>*>(x) + row * m;
 #pragma unroll
-  for (int q = 0; q < Eng::E; q++) v[q] = valid ? xc[t + TT * q] : mk<T>(T(0), T(0));
+  for (int q = 0; q < Eng::E; q++) {
+    if (valid) {
+      const cplx<Io> w = xc[t + TT * q];
+      v[q] = mk<T>(from_io<T>(w.x), from_io<T>(w.y));
+    } else {
+      v[q] = mk<T>(T(0), T(0));
+    }
+  }
   __syncthreads();
   cplx<T>* buf = bufs + rb * pitch;
   pm.template run<T, false>(v, buf, t, tw, 2);
@@ -95,8 +105,10 @@ __global__ void __launch_bounds__(kP2Threads)
 // Last axis, inverse: n/2+1 complex -> n reals (unnormalised).
 template <typename T, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
-    rows_c2r_p2(const cplx<T>* __restrict__ X, T* __restrict__ x, int64_t nrows, int H,
-                Eng pm, const cplx<T>* __restrict__ tw_g, int RB, int pitch, BatchMask mask) {
+    rows_c2r_p2(const cplx<T>* __restrict__ X, typename IoOf<T>::type* __restrict__ x,
+                int64_t nrows, int H, Eng pm, const cplx<T>* __restrict__ tw_g, int RB,
+                int pitch, BatchMask mask) {
+  using Io = typename IoOf<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -128,9 +140,9 @@ __global__ void __launch_bounds__(kP2Threads)
   }
   pm.template run<T, true>(v, bufs + rb * pitch, t, tw, 2);
   if (!valid) return;
-  cplx<T>* xc = reinterpret_cast<cplx<T>*>(x) + row * m;
+  cplx<Io>* xc = reinterpret_cast<cplx<Io>*>(x) + row * m;
 #pragma unroll
-  for (int q = 0; q < Eng::E; q++) xc[t + TT * q] = v[q];
+  for (int q = 0; q < Eng::E; q++) xc[t + TT * q] = mk<Io>(to_io<T>(v[q].x), to_io<T>(v[q].y));
 }
 
 // Middle axis: complex [A][n][B], lines along n; TB consecutive inner
@@ -268,21 +280,21 @@ __global__ void __launch_bounds__(kP2FusedThreads)
       k1 = (int)b;
     }
   }
-  const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
-          psi1 = __ldg(fp.tab.kpsi[1] + k1);
+  const T phi1 = ldg_val(fp.tab.kphi[1] + k1), chi1 = ldg_val(fp.tab.kchi[1] + k1),
+          psi1 = ldg_val(fp.tab.kpsi[1] + k1);
   T phi2 = T(1), chi2 = T(1), psi2 = T(1);
   if constexpr (DIM == 3) {
-    phi2 = __ldg(fp.tab.kphi[2] + k2);
-    chi2 = __ldg(fp.tab.kchi[2] + k2);
-    psi2 = __ldg(fp.tab.kpsi[2] + k2);
+    phi2 = ldg_val(fp.tab.kphi[2] + k2);
+    chi2 = ldg_val(fp.tab.kchi[2] + k2);
+    psi2 = ldg_val(fp.tab.kpsi[2] + k2);
   }
   // Per-line products of the axis-1/axis-2 factors (2D: axis 1 only).
   LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
 #pragma unroll
   for (int q = 0; q < Eng::E; q++) {
     const int k0 = t + p0.T() * q;
-    const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
-            psi0 = __ldg(fp.tab.kpsi[0] + k0);
+    const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
+            psi0 = ldg_val(fp.tab.kpsi[0] + k0);
     cplx<T> u[DIM];
 #pragma unroll
     for (int c = 0; c < DIM; c++) u[c] = v[c][q];
@@ -358,20 +370,20 @@ __global__ void __launch_bounds__(kP2Threads)
       k1 = (int)b;
     }
   }
-  const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
-          psi1 = __ldg(fp.tab.kpsi[1] + k1);
+  const T phi1 = ldg_val(fp.tab.kphi[1] + k1), chi1 = ldg_val(fp.tab.kchi[1] + k1),
+          psi1 = ldg_val(fp.tab.kpsi[1] + k1);
   T phi2 = T(1), chi2 = T(1), psi2 = T(1);
   if constexpr (DIM == 3) {
-    phi2 = __ldg(fp.tab.kphi[2] + k2);
-    chi2 = __ldg(fp.tab.kchi[2] + k2);
-    psi2 = __ldg(fp.tab.kpsi[2] + k2);
+    phi2 = ldg_val(fp.tab.kphi[2] + k2);
+    chi2 = ldg_val(fp.tab.kchi[2] + k2);
+    psi2 = ldg_val(fp.tab.kpsi[2] + k2);
   }
   const LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
 #pragma unroll 2
   for (int q = 0; q < Eng::E; q++) {
     const int k0 = t + p0.T() * q;
-    const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
-            psi0 = __ldg(fp.tab.kpsi[0] + k0);
+    const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
+            psi0 = ldg_val(fp.tab.kpsi[0] + k0);
     cplx<T> u[DIM];
 #pragma unroll
     for (int c = 0; c < DIM; c++) u[c] = stash[((size_t)c * TB + tb) * spitch + k0];
@@ -456,10 +468,10 @@ __global__ void __launch_bounds__(256)
     k1 = (int)(b / fp.H);
     k2 = (int)(b - (int64_t)k1 * fp.H);
   }
-  const T phi1 = __ldg(fp.tab.kphi[1] + k1), chi1 = __ldg(fp.tab.kchi[1] + k1),
-          psi1 = __ldg(fp.tab.kpsi[1] + k1);
-  const T phi2 = __ldg(fp.tab.kphi[2] + k2), chi2 = __ldg(fp.tab.kchi[2] + k2),
-          psi2 = __ldg(fp.tab.kpsi[2] + k2);
+  const T phi1 = ldg_val(fp.tab.kphi[1] + k1), chi1 = ldg_val(fp.tab.kchi[1] + k1),
+          psi1 = ldg_val(fp.tab.kpsi[1] + k1);
+  const T phi2 = ldg_val(fp.tab.kphi[2] + k2), chi2 = ldg_val(fp.tab.kchi[2] + k2),
+          psi2 = ldg_val(fp.tab.kpsi[2] + k2);
   const LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
   // One second of global time per wait; a wait that runs out is counted,
   // the tile is neither transformed nor stored, and the CTA waits (bounded
@@ -485,8 +497,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int q = 0; q < Eng::E; q++) {
       const int k0 = t + p0.T() * q;
-      const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
-              psi0 = __ldg(fp.tab.kpsi[0] + k0);
+      const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
+              psi0 = ldg_val(fp.tab.kpsi[0] + k0);
       cplx<T> u[DIM];
 #pragma unroll
       for (int c = 0; c < DIM; c++) u[c] = v[c][q];
@@ -515,8 +527,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll 2
     for (int q = 0; q < Eng::E; q++) {
       const int k0 = t + p0.T() * q;
-      const T phi0 = __ldg(fp.tab.kphi[0] + k0), chi0 = __ldg(fp.tab.kchi[0] + k0),
-              psi0 = __ldg(fp.tab.kpsi[0] + k0);
+      const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
+              psi0 = ldg_val(fp.tab.kpsi[0] + k0);
       cplx<T> u[DIM];
 #pragma unroll
       for (int c = 0; c < DIM; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
@@ -549,11 +561,11 @@ __global__ void __launch_bounds__(256)
 // geometry and returns false, launching nothing, when the length has no
 // compile-time instance.
 template <typename T>
-bool ct_rows_r2c(int m, const T* x, cplx<T>* X, int64_t nrows, int H, const cplx<T>* tw,
-                 BatchMask mask, cudaStream_t st);
+bool ct_rows_r2c(int m, const typename IoOf<T>::type* x, cplx<T>* X, int64_t nrows, int H,
+                 const cplx<T>* tw, BatchMask mask, cudaStream_t st);
 template <typename T>
-bool ct_rows_c2r(int m, const cplx<T>* X, T* x, int64_t nrows, int H, const cplx<T>* tw,
-                 BatchMask mask, cudaStream_t st);
+bool ct_rows_c2r(int m, const cplx<T>* X, typename IoOf<T>::type* x, int64_t nrows, int H,
+                 const cplx<T>* tw, BatchMask mask, cudaStream_t st);
 template <typename T, bool INV>
 bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw,
                  BatchMask mask, cudaStream_t st);
@@ -571,6 +583,14 @@ bool ct_axis0_stiffness_tma_f32(int n0, bool keep, cplx<float>* X, int64_t P, in
                                 int64_t bstride, int batch, const FusedParams<float>& fp,
                                 BatchMask mask, cudaStream_t st);
 void ct_set_smem_attrs_tma_f32(size_t max_smem);
+// Float-pair instances (passes_ct_df.cu, passes_df_rows.cu, passes_df_c2c.cu):
+// the staged and TMA axis-0 forms, rows and axis-1 passes, lengths 64..512.
+bool ct_axis0_stiffness_tma_df(int n0, cplx<df64>* X, int64_t P, int64_t cstride,
+                               int64_t bstride, int batch, const FusedParams<df64>& fp,
+                               BatchMask mask, cudaStream_t st);
+void ct_set_smem_attrs_df_axis0(size_t max_smem);
+void ct_set_smem_attrs_df_rows(size_t max_smem);
+void ct_set_smem_attrs_df_c2c(size_t max_smem);
 void ct_set_smem_attrs(size_t max_smem);
 
 }  // namespace bri17gb

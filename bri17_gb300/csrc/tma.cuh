@@ -106,8 +106,9 @@ bool encode_tiled_map_3d(CUtensorMap* map, const void* base, int elem_bytes, uin
                          uint64_t dim1, uint64_t dim2, uint64_t stride1_bytes,
                          uint64_t stride2_bytes, uint32_t box0, uint32_t box1);
 
-// Bounded waits that ran out in the FP32 TMA kernels since the last call
+// Bounded waits that ran out in the FP32 / float-pair TMA kernels since the last call
 // (read and cleared on the current device).
 cudaError_t tma_wait_timeouts_f32(int* count);
+cudaError_t tma_wait_timeouts_df(int* count);
 
 }  // namespace bri17gb

@@ -120,13 +120,29 @@ int bri17_op_set_material(bri17_op* op, double mu, double nu);
  * Form of the fused axis-0 stiffness pass (diagnostics; no reference
  * counterpart): 0 register-resident, 1 shared-memory staged, 2 TMA-staged
  * (tensor copies of whole tiles; FP32, 3D, even shape[1]), 3 TMA-staged with
- * the spectra kept in registers between the transforms.  FP32 handles
+ * the spectra kept in registers between the transforms (float-pair
+ * handles: 1 or 2, other values select 1).  FP32 handles
  * pick the fastest by timing at creation.  A form that does not apply to the
  * handle's grid falls back to the next applicable one at launch.  Results
  * agree between forms to rounding.
  */
 int bri17_op_fused_form(const bri17_op* op, int* form);
 int bri17_op_set_fused_form(bri17_op* op, int form);
+
+/*
+ * Float-pair arithmetic (no reference counterpart): on an FP64 handle,
+ * bri17_apply_stiffness and bri17_apply_stiffness_host compute in pairs of
+ * floats (hi + lo, 48-bit significands, error-free transformations on the
+ * FP32 pipe, which GB300 runs at about 60x its FP64 rate) with FP64 fields
+ * in memory.  Relative error against the FP64 operator is about 1e-14,
+ * within the 1e-12 parity bound of the FP64 path.  Values keep their 48 bits
+ * for magnitudes 1e-30..1e37.  3D power-of-two grids only: shape[0] and
+ * shape[1] in 64..512, shape[2] in 128..1024 (else
+ * BRI17_ERR_UNSUPPORTED_SIZE).  The other entry points of the handle
+ * (strain, right-hand side, CG, per-mode batches) stay in FP64.  Off by
+ * default.
+ */
+int bri17_op_set_float_pair(bri17_op* op, int enable);
 
 /*
  * Bounded device-side waits (tensor-copy completions) that ran out on the

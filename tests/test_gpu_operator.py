@@ -264,3 +264,60 @@ def test_tma_form_64_cubed():
     f = h.apply_stiffness(to_dev(u)).cpu().numpy().astype(np.float64)
     assert rel_l2(f, O.apply_stiffness(ho, u.astype(np.float64))) <= TOL_F32
     assert wait_timeouts() == 0
+
+
+# Float-pair arithmetic on FP64 handles (hi + lo floats, 48-bit
+# significands): the FP64 parity bound of 1e-12 against the oracle, both
+# axis-0 forms, field magnitudes far from 1, host buffers, rejected grids.
+FLOAT_PAIR_SHAPES = [
+    ((64, 64, 128), (1.0, 1.0, 1.0), 1.0, 0.25),
+    ((128, 128, 128), (1.0, 1.0, 1.0), 1.0, 0.25),
+    ((64, 256, 256), (1.0, 2.0, 0.5), 0.8, 0.35),
+    ((512, 64, 128), (1.0, 1.0, 0.125), 1.0, 0.35),
+]
+
+
+@pytest.mark.parametrize("shape,L,mu,nu", FLOAT_PAIR_SHAPES)
+def test_float_pair_operator_matches_oracle(shape, L, mu, nu):
+    import torch
+    from bri17_gb300 import wait_timeouts
+    h, ho = pair(shape, L, mu, nu)
+    rng = np.random.default_rng(21)
+    u = mean_free_normal(rng, 3, shape)
+    ud = to_dev(u)
+    f64 = h.apply_stiffness(ud)
+    h.set_float_pair(True)
+    f_ref = O.apply_stiffness(ho, u)
+    for form in ("staged", "tma"):
+        h.fused_form = form
+        f = h.apply_stiffness(ud)
+        torch.cuda.synchronize()
+        assert rel_l2(f.cpu().numpy(), f_ref) <= TOL_F64, form
+        assert float((f - f64).norm() / f64.norm()) <= 1e-13, form
+    assert wait_timeouts() == 0
+    for scale in (1e-12, 1e12):
+        f = h.apply_stiffness(ud * scale)
+        assert rel_l2(f.cpu().numpy(), f_ref * scale) <= TOL_F64, scale
+    h.set_float_pair(False)
+    assert torch.equal(h.apply_stiffness(ud), f64)
+
+
+def test_float_pair_host_buffers_and_rejected_grids():
+    import torch
+    from bri17_gb300._lib import Bri17Error
+    shape = (64, 64, 128)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3)
+    h.set_float_pair(True)
+    rng = np.random.default_rng(22)
+    u = mean_free_normal(rng, 3, shape)
+    f_ref = O.apply_stiffness(ho, u)
+    assert rel_l2(h.apply_stiffness_host(u), f_ref) <= TOL_F64
+    up = torch.from_numpy(u).pin_memory()
+    assert rel_l2(h.apply_stiffness_host(up).numpy(), f_ref) <= TOL_F64
+    for bad in ((48, 64, 128), (64, 64, 64), (32, 64, 128)):
+        hb, _ = pair(bad, (1.0, 1.0, 1.0), 1.0, 0.3)
+        with pytest.raises(Bri17Error):
+            hb.set_float_pair(True)
+    h32, _ = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3, precision="f32")
+    with pytest.raises(Bri17Error):
+        h32.set_float_pair(True)
