@@ -280,6 +280,18 @@ def float_pair_line(hooke, us, fs, nrot, args, dof, stream, u_host, f_host, hbm_
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / max(1, args.steps)
     diff = float((hooke.apply_stiffness(us[0]) - ref).norm() / ref.norm())
+    # Per-pass device times (events between the passes).
+    L.bri17_op_set_pass_timing(hooke.handle, 1)
+    for i in range(args.steps):
+        hooke.apply_stiffness(us[i % nrot], out=fs[i % nrot])
+    torch.cuda.synchronize()
+    pms = (C.c_double * 16)()
+    pn = (C.c_int64 * 16)()
+    npass = C.c_int()
+    L.bri17_op_pass_times(hooke.handle, pms, pn, 16, C.byref(npass))
+    L.bri17_op_set_pass_timing(hooke.handle, 0)
+    passes = {L.bri17_pass_name(i).decode(): round(pms[i] / pn[i], 5)
+              for i in range(min(16, npass.value)) if pn[i] > 0}
     sp = C.c_void_p(stream.cuda_stream)
     for _ in range(max(1, args.warmup)):
         L.bri17_apply_stiffness_host(hooke.handle, C.c_void_p(u_host.data_ptr()),
@@ -296,7 +308,7 @@ def float_pair_line(hooke, us, fs, nrot, args, dof, stream, u_host, f_host, hbm_
             "rel_diff_vs_f64_operator": diff,
             "operator_hbm_frac": 16 * dof / (ms * 1e-3) / 1e9 / hbm_peak,
             "e2e": {"value": dof * args.steps / e2e_s / 1e9, "unit": "GDoF/s"},
-            "axis0_form": form}
+            "axis0_form": form, "pass_ms": passes}
 
 
 def config_of(w, ngpus, precision="f64"):

@@ -120,8 +120,9 @@ __device__ __forceinline__ typename IoOf<T>::type to_io(T v) {
 // double -> hi + lo without the FP64 pipe: the 53-bit significand is split
 // by integer operations into its top 24 bits rounded to nearest even (hi)
 // and the signed remainder (lo, rounded to 24 bits), each scaled by an
-// exact power of two.  Zeros and subnormal doubles give 0; infinities and
-// NaN give hi = the value converted to float, lo = 0.
+// exact power of two; integer operations only.  Zeros and subnormal doubles
+// give a signed zero, infinities infinity, NaN a NaN, and magnitudes beyond
+// the float range infinity.
 __device__ __forceinline__ float df_pow2(int e) {
   // 2^e for e in [-149, 127] (subnormal range included), built exactly.
   if (e >= -126) return __int_as_float((e + 127) << 23);
@@ -133,8 +134,11 @@ __device__ __forceinline__ df64 from_io<df64>(double v) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int ex = (int)((bits >> 52) & 0x7FF);
   const bool neg = (bits >> 63) != 0;
-  if (ex == 0) return df64(0.f, 0.f);
-  if (ex == 0x7FF) return df64(__double2float_rn(v), 0.f);
+  const unsigned fsign = neg ? 0x80000000u : 0u;
+  if (ex == 0) return df64(__uint_as_float(fsign), 0.f);
+  if (ex == 0x7FF)  // infinity, or a quiet NaN
+    return df64(__uint_as_float(fsign | 0x7F800000u | ((bits & ((1ull << 52) - 1)) ? 0x400000u : 0u)),
+                0.f);
   const long long sig = (long long)((bits & ((1ull << 52) - 1)) | (1ull << 52));
   long long q = sig >> 29;              // top 24 bits
   long long r = sig & ((1ll << 29) - 1);  // low 29 bits
@@ -146,24 +150,60 @@ __device__ __forceinline__ df64 from_io<df64>(double v) {
   const int eh = ex - 1046, el = ex - 1075;
   float hi, lo;
   if (eh > 127 - 24) {
-    hi = __double2float_rn(v);  // beyond the float range: overflow as a float would
+    hi = __uint_as_float(0x7F800000u);  // beyond the float range: infinity
     lo = 0.f;
   } else {
     // q <= 2^24 and |r| <= 2^28 convert to float (q exactly, r rounded);
     // the power-of-two scalings are exact unless they underflow.
+    // (32-bit integer conversions: the 64-bit ones do not run on the FP32
+    // side.)
     const float sh = eh >= -149 ? df_pow2(eh) : 0.f;
-    hi = __fmul_rn(__ll2float_rn(q), sh);
+    hi = __fmul_rn(__int2float_rn((int)q), sh);
     // Split the scaling of lo so that neither factor underflows early.
     const int el1 = el < -126 ? -126 : el;
-    lo = __fmul_rn(__fmul_rn(__ll2float_rn(r), df_pow2(el1)),
+    lo = __fmul_rn(__fmul_rn(__int2float_rn((int)r), df_pow2(el1)),
                    el < -126 ? (el - el1 >= -149 ? df_pow2(el - el1) : 0.f) : 1.f);
   }
   return neg ? df64(-hi, -lo) : df64(hi, lo);
 }
 
+// hi + lo -> double by integer operations only (float-to-double conversions
+// and the add would run on the FP64 pipe): hi's 24-bit significand goes to
+// the top of 53 bits, lo's is added or subtracted at its offset (bits below
+// the 53 are dropped: error below 2^-52 relative), then one normalisation.
+// Zero or subnormal hi gives a signed zero; an infinite or NaN part gives
+// infinity or NaN.
 template <>
 __device__ __forceinline__ double to_io<df64>(df64 v) {
-  return __dadd_rn((double)v.hi, (double)v.lo);
+  const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const int eh = (int)((hb >> 23) & 0xFF), el = (int)((lb >> 23) & 0xFF);
+  unsigned long long sign = (unsigned long long)(hb >> 31) << 63;
+  if (eh == 0xFF || el == 0xFF) {
+    const unsigned long long nan = (el == 0xFF && (lb & 0x7FFFFFu)) ? (1ull << 51) : 0;
+    return __longlong_as_double((long long)(sign | (0x7FFull << 52) |
+                                            ((unsigned long long)(hb & 0x7FFFFFu) << 29) | nan));
+  }
+  if (eh == 0) return __longlong_as_double((long long)sign);
+  long long M = (long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
+  const int shift = eh - el;
+  if (el != 0) {
+    long long L = (long long)((lb & 0x7FFFFFu) | 0x800000u);
+    L = shift <= 29 ? (L << (29 - shift)) : (shift - 29 < 62 ? (L >> (shift - 29)) : 0);
+    M = ((hb ^ lb) >> 31) == 0 ? M + L : M - L;
+  }
+  if (M == 0) return __longlong_as_double((long long)sign);
+  if (M < 0) {
+    M = -M;
+    sign ^= 1ull << 63;
+  }
+  // Put the leading bit at position 52.
+  const int lead = 63 - __clzll(M);
+  int e = eh - 127 + 1023 + (lead - 52);
+  M = lead >= 52 ? (M >> (lead - 52)) : (M << (52 - lead));
+  if (e <= 0) return __longlong_as_double((long long)sign);
+  if (e >= 0x7FF) return __longlong_as_double((long long)(sign | (0x7FFull << 52)));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)e << 52) | ((unsigned long long)M & ((1ull << 52) - 1))));
 }
 
 }  // namespace bri17gb

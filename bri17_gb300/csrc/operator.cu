@@ -431,6 +431,21 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
   return BRI17_OK;
 }
 
+// BRI17_FUSED_FORM=registers|staged|tma|tma_registers overrides the
+// per-handle choice of the axis-0 form (for measurements); -1 when unset.
+static int env_fused_form() {
+  static const int form = [] {
+    const char* e = getenv("BRI17_FUSED_FORM");
+    if (!e) return -1;
+    return strcmp(e, "registers") == 0       ? 0
+           : strcmp(e, "staged") == 0        ? 1
+           : strcmp(e, "tma") == 0           ? 2
+           : strcmp(e, "tma_registers") == 0 ? 3
+                                             : -1;
+  }();
+  return form;
+}
+
 template <typename T, int DIM, int MODE>
 static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
                         int64_t bstride, const FusedParams<T>& fp, BatchMask mask,
@@ -444,15 +459,7 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
     // Form chosen per handle (fused_form, autotuned at creation for FP32);
     // BRI17_FUSED_FORM=registers|staged|tma|tma_registers overrides it (for measurements).
     // A form whose launcher declines the size falls through to the next.
-    static const int env_form = [] {
-      const char* e = getenv("BRI17_FUSED_FORM");
-      if (!e) return -1;
-      return strcmp(e, "registers") == 0       ? 0
-             : strcmp(e, "staged") == 0        ? 1
-             : strcmp(e, "tma") == 0           ? 2
-             : strcmp(e, "tma_registers") == 0 ? 3
-                                               : -1;
-    }();
+    const int env_form = env_fused_form();
     const int form = env_form >= 0 ? env_form : fp.form;
     if constexpr (std::is_same<T, float>::value && DIM == 3) {
       if ((form == 2 || form == 3) &&
@@ -1192,6 +1199,7 @@ extern "C" int bri17_modal_eigenstress_to_opposite_strain_batch(
 // only).  `form` selects the axis-0 pass: 2 TMA-staged, else staged.
 static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
                             cudaStream_t st) {
+  if (env_fused_form() >= 0) form = env_fused_form();
   const Geometry& g = op->g;
   const int dim = g.dim;
   const Tables<df64>& tab = op->tabdf;
