@@ -65,6 +65,7 @@ _SIGS = {
     "bri17_op_set_fused_form": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_wait_timeouts": ([c_int_p], ctypes.c_int),
     "bri17_op_set_float_pair": ([vp, ctypes.c_int], ctypes.c_int),
+    "bri17_eigenstress_to_opposite_strain": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_op_set_pass_timing": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_op_pass_times": ([vp, c_double_p, c_int64_p, ctypes.c_int, c_int_p], ctypes.c_int),
     "bri17_pass_name": ([ctypes.c_int], ctypes.c_char_p),

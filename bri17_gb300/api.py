@@ -296,6 +296,21 @@ class Hooke:
             _stream_ptr(stream)), "bri17_eigenstress_rhs")
         return b
 
+    def eigenstress_to_opposite_strain(self, tau, stream=None):
+        """Opposite strain eta = -eps (sym, *shape) of a cell-wise Mandel
+        eigenstress tau (sym, *shape): the field form of
+        Hooke::modal_eigenstress_to_opposite_strain as python/demo.py applies
+        it mode by mode (the direct solution of the eigenstress problem)."""
+        torch = _torch()
+        d = self._grid.dim
+        sym = 3 if d == 2 else 6
+        tau = self._field(tau, sym)
+        eta = torch.empty((sym,) + self._grid.shape, dtype=self.dtype, device=tau.device)
+        check(_lib.load().bri17_eigenstress_to_opposite_strain(
+            self._h, ctypes.c_void_p(tau.data_ptr()), ctypes.c_void_p(eta.data_ptr()),
+            _stream_ptr(stream)), "bri17_eigenstress_to_opposite_strain")
+        return eta
+
     def cg_solve(self, b, x0=None, tol: float = 1e-8, max_iterations: int = 100000,
                  mode: str = "plain", raise_on_failure: bool = True, stream=None):
         """Solve K x = b (zero-mean x) by CG.  b: FP64 CUDA tensor (DIM,

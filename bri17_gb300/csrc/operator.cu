@@ -216,6 +216,8 @@ static void set_smem_attrs() {
     SET_FUSED(3, kModeStrain);
     SET_FUSED(2, kModeRhs);
     SET_FUSED(3, kModeRhs);
+    SET_FUSED(2, kModeSolve);
+    SET_FUSED(3, kModeSolve);
 #undef SET_FUSED
     cudaGetLastError();
   });
@@ -451,8 +453,8 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
                         int64_t bstride, const FusedParams<T>& fp, BatchMask mask,
                         cudaStream_t st) {
   constexpr int SYM = DIM == 2 ? 3 : 6;
-  constexpr int CIN = MODE == kModeRhs ? SYM : DIM;
-  constexpr int COUT = MODE == kModeStrain ? SYM : DIM;
+  constexpr int CIN = (MODE == kModeRhs || MODE == kModeSolve) ? SYM : DIM;
+  constexpr int COUT = (MODE == kModeStrain || MODE == kModeSolve) ? SYM : DIM;
   constexpr int CMAX = CIN > COUT ? CIN : COUT;
   if (MODE == kModeStiffness && g.use_p8[0]) {
     const Plan8& p = g.p8[0];
@@ -509,9 +511,13 @@ static FusedParams<T> fused_params(const bri17_op* op, const Tables<T>& tab,
   fp.n1 = op->g.dim == 3 ? op->g.n[1] : 1;
   fp.H = op->g.H;
   const double scaling = op->mu / (1. - 2. * op->nu);
-  fp.s = (T)(scaling * op->corr);
-  fp.mu = (T)(op->mu * op->corr);
-  fp.corr = mode == kModeStrain ? (T)(1.0 / (double)op->g.size) : (T)op->corr;
+  // The solve mode inverts the reference's unscaled K(k) and normalises the
+  // inverse transform by 1/|N|, as the strain mode does.
+  const double kscale = mode == kModeSolve ? 1.0 : op->corr;
+  fp.s = (T)(scaling * kscale);
+  fp.mu = (T)(op->mu * kscale);
+  fp.corr = (mode == kModeStrain || mode == kModeSolve) ? (T)(1.0 / (double)op->g.size)
+                                                        : (T)op->corr;
   fp.mat = nullptr;
   fp.form = op->fused_form;
   return fp;
@@ -593,8 +599,8 @@ static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
   const Geometry& g = op->g;
   const int dim = g.dim;
   const int sym = dim == 2 ? 3 : 6;
-  const int cin = MODE == kModeRhs ? sym : dim;
-  const int cout = MODE == kModeStrain ? sym : dim;
+  const int cin = (MODE == kModeRhs || MODE == kModeSolve) ? sym : dim;
+  const int cout = (MODE == kModeStrain || MODE == kModeSolve) ? sym : dim;
   const int cmax = cin > cout ? cin : cout;
   const int nlast = g.n[dim - 1];
   const int64_t rows_per_comp = g.size / nlast;
@@ -1571,6 +1577,25 @@ extern "C" int bri17_eigenstress_rhs(bri17_op* op, const void* tau, void* b,
   int rc = ensure_spectrum(op, sym);
   if (rc != BRI17_OK) return rc;
   return eigenstress_rhs_batched_async(op, 1, tau, b, op->spec, (cudaStream_t)stream);
+}
+
+extern "C" int bri17_eigenstress_to_opposite_strain(bri17_op* op, const void* tau, void* eta,
+                                                    void* stream) {
+  if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
+  if (!tau || !eta) return invalid("null pointer");
+  const int sym = op->g.dim == 2 ? 3 : 6;
+  int rc = ensure_spectrum(op, sym);
+  if (rc != BRI17_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (op->precision == BRI17_F64)
+    return run_pipeline<double, kModeSolve>(op, op->tab64, (const double*)tau, (double*)eta, 1,
+                                            op->spec, nullptr, st);
+  return run_pipeline<float, kModeSolve>(op, op->tab32, (const float*)tau, (float*)eta, 1,
+                                         op->spec, nullptr, st);
 }
 
 extern "C" int bri17_op_fused_form(const bri17_op* op, int* form) {

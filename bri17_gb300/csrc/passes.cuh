@@ -24,7 +24,9 @@ namespace bri17gb {
 
 constexpr int kThreads = 256;
 
-enum FusedMode { kModeStiffness = 0, kModeStrain = 1, kModeRhs = 2 };
+// kModeSolve: eigenstress -> opposite strain, the field form of
+// Hooke::modal_eigenstress_to_opposite_strain (include/bri17/bri17.hpp:308-355).
+enum FusedMode { kModeStiffness = 0, kModeStrain = 1, kModeRhs = 2, kModeSolve = 3 };
 
 // Optional per-batch-entry mask: a CTA whose work belongs to entry z exits
 // at once when flags[z * stride] == 0.  `unit` is the number of CTA work
@@ -250,6 +252,69 @@ __device__ __forceinline__ void stiffness2(T phi0, T chi0, T psi0, T phi1,
   u[1] = mk<T>(K01 * u0.x + K11 * u1.x, K01 * u0.y + K11 * u1.y);
 }
 
+// The real symmetric K(k) itself (same products as stiffness3/stiffness2),
+// row-major DIM x DIM.
+template <typename T, int DIM>
+__device__ __forceinline__ void stiffness_matrix(const T* phi, const T* chi, const T* psi, T s,
+                                                 T mu, T* K) {
+  if constexpr (DIM == 3) {
+    const T H00 = phi[0] * chi[1] * chi[2];
+    const T H11 = chi[0] * phi[1] * chi[2];
+    const T H22 = chi[0] * chi[1] * phi[2];
+    const T Kd = mu * (H00 + H11 + H22);
+    K[0] = s * H00 + Kd;
+    K[4] = s * H11 + Kd;
+    K[8] = s * H22 + Kd;
+    K[1] = K[3] = s * psi[0] * psi[1] * chi[2];
+    K[2] = K[6] = s * psi[0] * chi[1] * psi[2];
+    K[5] = K[7] = s * chi[0] * psi[1] * psi[2];
+  } else {
+    const T H00 = phi[0] * chi[1];
+    const T H11 = chi[0] * phi[1];
+    const T Kd = mu * (H00 + H11);
+    K[0] = s * H00 + Kd;
+    K[3] = s * H11 + Kd;
+    K[1] = K[2] = s * psi[0] * psi[1];
+  }
+}
+
+// Solves K u = r for a real symmetric positive definite K (DIM x DIM,
+// row-major) and complex r, by LDL^T (the reference's Eigen LLT,
+// include/bri17/bri17.hpp:341, in a square-root-free form).
+template <typename T, int DIM>
+__device__ __forceinline__ void spd_solve(const T* K, const cplx<T>* r, cplx<T>* u) {
+  T L[DIM][DIM], D[DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; j++) {
+    T d = K[j * DIM + j];
+#pragma unroll
+    for (int p = 0; p < j; p++) d -= L[j][p] * L[j][p] * D[p];
+    D[j] = d;
+#pragma unroll
+    for (int i = j + 1; i < DIM; i++) {
+      T v = K[i * DIM + j];
+#pragma unroll
+      for (int p = 0; p < j; p++) v -= L[i][p] * L[j][p] * D[p];
+      L[i][j] = v / d;
+    }
+  }
+  cplx<T> y[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; i++) {
+    cplx<T> v = r[i];
+#pragma unroll
+    for (int p = 0; p < i; p++) v = csub<T>(v, cscale<T>(y[p], L[i][p]));
+    y[i] = v;
+  }
+#pragma unroll
+  for (int i = DIM - 1; i >= 0; i--) {
+    cplx<T> v = cscale<T>(y[i], T(1) / D[i]);
+#pragma unroll
+    for (int p = i + 1; p < DIM; p++) v = csub<T>(v, cscale<T>(u[p], L[p][i]));
+    u[i] = v;
+  }
+}
+
 // Modal strain-displacement vector (include/bri17/bri17.hpp:212-236):
 // B_i = 2 i e^{i sum alpha} s_i prod_{j != i} c_j.
 template <typename T, int DIM>
@@ -294,8 +359,8 @@ __global__ void __launch_bounds__(kThreads)
                 int64_t bstride, int TB, int pitch, AxisPlan p0,
                 FusedParams<T> fp, BatchMask mask) {
   constexpr int SYM = DIM == 2 ? 3 : 6;
-  constexpr int CIN = MODE == kModeRhs ? SYM : DIM;
-  constexpr int COUT = MODE == kModeStrain ? SYM : DIM;
+  constexpr int CIN = (MODE == kModeRhs || MODE == kModeSolve) ? SYM : DIM;
+  constexpr int COUT = (MODE == kModeStrain || MODE == kModeSolve) ? SYM : DIM;
   constexpr int CMAX = CIN > COUT ? CIN : COUT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -367,7 +432,50 @@ __global__ void __launch_bounds__(kThreads)
       }
       cplx<T> B[DIM];
       bvec<T, DIM>(cc, ss, e, B);
-      if constexpr (MODE == kModeStrain) {
+      if constexpr (MODE == kModeSolve) {
+        // eta_hat = corr * sym(B (x) u), u = K^-1 (tau_mat . conj(B)); k = 0
+        // gives 0 (include/bri17/bri17.hpp:333-354).
+        cplx<T> tau[SYM];
+#pragma unroll
+        for (int q = 0; q < SYM; q++) tau[q] = buf[q * TB * pitch + off];
+        const T ir2 = T(0.7071067811865475244008443621048490392848);
+        const T r2 = T(1.414213562373095048801688724209698079);
+        cplx<T> rhs[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; d++) rhs[d] = mk<T>(T(0), T(0));
+#pragma unroll
+        for (int q = 0; q < SYM; q++) {
+          int i, j;
+          mandel_pair<DIM>(q, i, j);
+          if (i == j) {
+            rhs[i] = cadd<T>(rhs[i], cmulc<T>(tau[q], B[i]));
+          } else {
+            const cplx<T> t = cscale<T>(tau[q], ir2);
+            rhs[i] = cadd<T>(rhs[i], cmulc<T>(t, B[j]));
+            rhs[j] = cadd<T>(rhs[j], cmulc<T>(t, B[i]));
+          }
+        }
+        const bool null_frequency = k0 == 0 && k1 == 0 && k2 == 0;
+        T phi[DIM], chi[DIM], psi[DIM], K[DIM * DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; d++) {
+          phi[d] = __ldg(fp.tab.kphi[d] + kk[d]);
+          chi[d] = __ldg(fp.tab.kchi[d] + kk[d]);
+          psi[d] = __ldg(fp.tab.kpsi[d] + kk[d]);
+        }
+        stiffness_matrix<T, DIM>(phi, chi, psi, s, mu, K);
+        cplx<T> u[DIM];
+        spd_solve<T, DIM>(K, rhs, u);
+#pragma unroll
+        for (int q = 0; q < SYM; q++) {
+          int i, j;
+          mandel_pair<DIM>(q, i, j);
+          cplx<T> v = cadd<T>(cmul<T>(B[i], u[j]), cmul<T>(u[i], B[j]));
+          const T w = (i == j ? T(0.5) : T(0.5) * r2) * fp.corr;
+          buf[q * TB * pitch + off] =
+              null_frequency ? mk<T>(T(0), T(0)) : cscale<T>(v, w);
+        }
+      } else if constexpr (MODE == kModeStrain) {
         // eps_hat = corr * sym(u (x) B), sqrt(2) on the shears
         // (tests/test_bri17.cpp:223-230).
         cplx<T> u[DIM];

@@ -199,6 +199,13 @@ class Hooke {
   void eigenstress_rhs(T const* tau_dev, T* b_dev, cudaStream_t s = nullptr) const {
     detail::check(bri17_eigenstress_rhs(op_, tau_dev, b_dev, s), "bri17_eigenstress_rhs");
   }
+  /** Opposite strain field of a Mandel eigenstress field: the whole-field
+   *  modal_eigenstress_to_opposite_strain (:308-355), sym x size. */
+  void eigenstress_to_opposite_strain(T const* tau_dev, T* eta_dev,
+                                      cudaStream_t s = nullptr) const {
+    detail::check(bri17_eigenstress_to_opposite_strain(op_, tau_dev, eta_dev, s),
+                  "bri17_eigenstress_to_opposite_strain");
+  }
   /** CG solve of K x = b (FP64 vectors); mixed = FP32 inner + FP64 refinement. */
   bri17_cg_info cg_solve(double const* b_dev, double* x_dev, double tol, int max_iterations,
                          bool mixed = false, cudaStream_t s = nullptr) const {

@@ -243,6 +243,18 @@ int bri17_apply_strain(bri17_op* op, const void* u_dev, void* eps_dev,
 int bri17_eigenstress_rhs(bri17_op* op, const void* tau_dev, void* b_dev,
                           void* stream);
 
+/*
+ * Opposite strain eta = -eps of a cell-wise eigenstress field tau: the
+ * whole-field form of Hooke::modal_eigenstress_to_opposite_strain
+ * (include/bri17/bri17.hpp:308-355) as python/demo.py:24-40 applies it mode
+ * by mode: eta = ifft(eta_hat(fft(tau))), eta_hat(k) = sym(B (x) K^-1
+ * (tau_hat . conj(B))) in Mandel form, eta_hat(0) = 0.  The direct
+ * (per-mode) solution of the eigenstress problem.  tau_dev, eta_dev:
+ * sym x size, the handle's precision (sym = 3 in 2D, 6 in 3D).
+ */
+int bri17_eigenstress_to_opposite_strain(bri17_op* op, const void* tau_dev,
+                                         void* eta_dev, void* stream);
+
 /* Conjugate-gradient modes. */
 typedef enum bri17_cg_mode {
   BRI17_CG_PLAIN = 0,        /* CG in the handle's precision */

@@ -427,6 +427,34 @@ void oracle_eigenstress_modal_solve(int dim, const int* shape, const double* L,
   }
 }
 
+/* Opposite strain in Fourier space over the full spectrum: eta_hat[k] =
+ * Hooke::modal_eigenstress_to_opposite_strain(k, tau_hat[k])
+ * (include/bri17/bri17.hpp:308-355), the per-mode loop of
+ * python/demo.py:34-40.  tauhat and etahat are sym x size complex (SoA). */
+void oracle_eigenstress_modal_eta(int dim, const int* shape, const double* L, double mu,
+                                  double nu, const double* tauhat, double* etahat) {
+  oracle_hooke h;
+  make_hooke(&h, dim, shape, L, mu, nu);
+  int64_t size = 1;
+  for (int i = 0; i < dim; i++) size *= shape[i];
+  const int sym = dim == 2 ? 3 : 6;
+#pragma omp parallel for schedule(static)
+  for (int64_t m = 0; m < size; m++) {
+    int k[3];
+    double tau[12], eta[12];
+    unflatten(&h, m, k);
+    for (int s = 0; s < sym; s++) {
+      tau[2 * s] = tauhat[2 * (s * size + m)];
+      tau[2 * s + 1] = tauhat[2 * (s * size + m) + 1];
+    }
+    eigenstress_solve(&h, k, tau, 0, eta);
+    for (int s = 0; s < sym; s++) {
+      etahat[2 * (s * size + m)] = eta[2 * s];
+      etahat[2 * (s * size + m) + 1] = eta[2 * s + 1];
+    }
+  }
+}
+
 /* Eigenstress right-hand side in Fourier space: b_hat[k] = tau_hat[k] .
  * conj(B(k)) (the rhs of include/bri17/bri17.hpp:340), DIM x size complex. */
 void oracle_eigenstress_modal_rhs(int dim, const int* shape, const double* L,

@@ -70,7 +70,8 @@ def lib() -> ctypes.CDLL:
                          "oracle_modal_strain_displacement_batch"):
                 getattr(L, name).argtypes = common + [_ip, ctypes.c_int64, _dp]
             for name in ("oracle_stiffness_modal_apply", "oracle_strain_modal_apply",
-                         "oracle_eigenstress_modal_solve", "oracle_eigenstress_modal_rhs"):
+                         "oracle_eigenstress_modal_solve", "oracle_eigenstress_modal_rhs",
+                         "oracle_eigenstress_modal_eta"):
                 getattr(L, name).argtypes = common + [_dp, _dp]
             L.oracle_get_cell_nodes.argtypes = [ctypes.c_int, _ip, ctypes.c_int, _ip]
             L.oracle_get_node_at.argtypes = [ctypes.c_int, _ip, _ip]
@@ -310,6 +311,19 @@ def eigenstress_solve(hooke: Hooke, tau):
     tauhat = np.fft.fftn(tau.astype(np.complex128), axes=_axes(g.dim))
     uhat = hooke._modal_loop(lib().oracle_eigenstress_modal_solve, tauhat, g.dim)
     return -np.fft.ifftn(uhat, axes=_axes(g.dim)).real
+
+
+def eigenstress_opposite_strain(hooke: Hooke, tau):
+    """Opposite strain field eta = ifft(eta_hat(fft(tau))) with eta_hat the
+    per-mode Hooke::modal_eigenstress_to_opposite_strain
+    (include/bri17/bri17.hpp:308-355) over every mode, as python/demo.py:24-40
+    runs it; (sym, *shape) real."""
+    g = hooke.grid
+    sym = 3 if g.dim == 2 else 6
+    tau = np.asarray(tau, dtype=np.float64).reshape((sym,) + g.shape)
+    tauhat = np.fft.fftn(tau.astype(np.complex128), axes=_axes(g.dim))
+    etahat = hooke._modal_loop(lib().oracle_eigenstress_modal_eta, tauhat, sym)
+    return np.fft.ifftn(etahat, axes=_axes(g.dim)).real
 
 
 def set_num_threads(n: int) -> None:

@@ -145,3 +145,29 @@ def test_wrong_device_and_dtype_are_rejected():
         h.apply_stiffness(torch.zeros((3, 8, 8, 7), dtype=torch.float64, device="cuda"))
     with pytest.raises(Bri17Error):
         h.set_material(1.0, 0.5)
+
+
+# Field form of Hooke::modal_eigenstress_to_opposite_strain (the direct
+# solution of the eigenstress problem, python/demo.py's per-mode loop on the
+# whole spectrum) against the oracle: FP64 at the operator's 1e-12 bound,
+# FP32 at its 2e-5; 2D and 3D, odd and power-of-two sides.
+OPP_SHAPES = [
+    ((16, 12), (1.0, 0.75), 1.0, 0.3),
+    ((8, 8, 8), (1.0, 1.0, 1.0), 1.0, 0.25),
+    ((7, 10, 6), (1.0, 2.0, 0.5), 0.7, 0.45),
+    ((32, 16, 24), (1.0, 1.0, 1.0), 1.3, 0.1),
+]
+
+
+@pytest.mark.parametrize("shape,L,mu,nu", OPP_SHAPES)
+def test_opposite_strain_field_matches_oracle(shape, L, mu, nu):
+    from gpu_helpers import pair, rel_l2, to_dev
+    sym = 3 if len(shape) == 2 else 6
+    rng = np.random.default_rng(31)
+    tau = rng.standard_normal((sym,) + shape)
+    for precision, tol in (("f64", 1e-12), ("f32", 2e-5)):
+        h, ho = pair(shape, L, mu, nu, precision=precision)
+        eta_ref = O.eigenstress_opposite_strain(ho, tau)
+        t = to_dev(tau.astype(np.float64 if precision == "f64" else np.float32))
+        eta = h.eigenstress_to_opposite_strain(t).cpu().numpy().astype(np.float64)
+        assert rel_l2(eta, eta_ref) <= tol, precision

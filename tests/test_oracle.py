@@ -173,3 +173,24 @@ def test_repr_strings_match_reference():
         expected = (f"Hooke<d,{dim}>{{mu={_fmt(mu)},nu={_fmt(nu)},grid="
                     f"{CartesianGrid(shape, L)!r}\n")
         assert expected == buf.value.decode()
+
+
+def test_opposite_strain_field_restatement():
+    """The field form of modal_eigenstress_to_opposite_strain agrees with the
+    per-mode restatement at a mode, and eta = -eps(u) for the direct
+    displacement solve u of the same eigenstress (include/bri17/bri17.hpp:300,
+    :342: the reference's modal u is the negative displacement)."""
+    g = O.Grid((6, 5, 4), (1.0, 1.2, 0.8))
+    h = O.Hooke(1.3, 0.3, g)
+    rng = np.random.default_rng(0)
+    tau = rng.standard_normal((6, 6, 5, 4))
+    eta = O.eigenstress_opposite_strain(h, tau)
+    tauhat = np.fft.fftn(tau.astype(complex), axes=(1, 2, 3))
+    etahat = np.fft.fftn(eta.astype(complex), axes=(1, 2, 3))
+    for k in ((2, 1, 3), (0, 0, 1), (5, 4, 2)):
+        e = h.modal_eigenstress_to_opposite_strain(np.array(k, dtype=np.intc),
+                                                   tauhat[(slice(None),) + k].copy())
+        assert np.abs(e - etahat[(slice(None),) + k]).max() <= 1e-13 * np.abs(etahat).max()
+    assert np.abs(etahat[:, 0, 0, 0]).max() <= 1e-13 * np.abs(etahat).max()
+    eps = O.apply_strain(h, O.eigenstress_solve(h, tau))
+    assert np.abs(eta + eps).max() <= 1e-13 * np.abs(eta).max()
