@@ -31,11 +31,108 @@ struct PE {
     return E == 8 ? ((LN % 3 == 1) ? (s < LN / 3 - 1 ? 8 : 4) : (s < LN / 3 ? 8 : 4))
                   : (s < LN / 4 ? 16 : (1 << (LN % 4)));
   }
+  // Product of the radices before stage s.
+  static constexpr int ns(int s) {
+    int p = 1;
+    for (int i = 0; i < s; i++) p *= radix(i);
+    return p;
+  }
+  // Per-stage twiddle table: stage s >= 1 holds W^(jm r tstep) at
+  // (r - 1) ns(s) + jm, r in [1, R), jm in [0, ns(s)), after the stages
+  // before it; stage 0 has none.  N - radix(0) entries in all.
+  static constexpr int twoff(int s) {
+    int o = 0;
+    for (int i = 1; i < s; i++) o += (radix(i) - 1) * ns(i);
+    return o;
+  }
+  static constexpr int TWN = N - (NST > 0 ? radix(0) : N);
 };
 
+// Fills the per-stage twiddle table of PE<N, E> from the natural table `tw`
+// (W_{N tws}^i at i, read with stride tws); cooperative over `nthr` threads.
+// Stage by stage at compile time, so the index arithmetic is shifts and
+// masks.
+template <typename T, int N, int E, int S>
+__device__ __forceinline__ void fftE_ct_twiddles_from(cplx<T>* __restrict__ dst,
+                                                      const cplx<T>* __restrict__ tw, int tws,
+                                                      int tid, int nthr) {
+  using P = PE<N, E>;
+  if constexpr (S < P::NST) {
+    constexpr int NS = P::ns(S), R = P::radix(S), OFF = P::twoff(S);
+    constexpr int STEP = N / (NS * R);
+    for (int i = tid; i < (R - 1) * NS; i += nthr) {
+      const int r = 1 + i / NS, jm = i % NS;
+      dst[OFF + i] = tw[jm * r * STEP * tws];
+    }
+    fftE_ct_twiddles_from<T, N, E, S + 1>(dst, tw, tws, tid, nthr);
+  }
+}
+
+template <typename T, int N, int E>
+__device__ __forceinline__ void fftE_ct_twiddles(cplx<T>* __restrict__ dst,
+                                                 const cplx<T>* __restrict__ tw, int tws,
+                                                 int tid, int nthr) {
+  fftE_ct_twiddles_from<T, N, E, 1>(dst, tw, tws, tid, nthr);
+}
+
+// One radix-R stage reading its twiddles from the per-stage table `stw`
+// (consecutive butterflies, consecutive entries: no bank conflicts).
+template <typename T, int R, int E, bool INV>
+__device__ __forceinline__ void stageE_st(cplx<T> (&v)[E], cplx<T>* buf, int t, int TT,
+                                          int Ns, const cplx<T>* __restrict__ stw, bool last) {
+  constexpr int M = E / R;
+#pragma unroll
+  for (int m = 0; m < M; m++) {
+    const int j = t + TT * m;
+    const int jm = j & (Ns - 1);
+    cplx<T> a[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) a[r] = v[m + r * M];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) a[r] = cmul<T>(a[r], twid<T, INV>(stw, (r - 1) * Ns + jm));
+    }
+    dft<T, R, INV>(a);
+    if (last) {
+#pragma unroll
+      for (int r = 0; r < R; r++) v[m + r * M] = a[r];
+    } else {
+      const int d = (j - jm) * R + jm;
+#pragma unroll
+      for (int r = 0; r < R; r++) buf[pad16(d + r * Ns)] = a[r];
+    }
+  }
+}
+
+// `stw`: the per-stage twiddle table (fftE_ct_twiddles).
 template <typename T, int N, int E, bool INV, int S, int NS>
 __device__ __forceinline__ void fftE_ct_stage(cplx<T> (&v)[E], cplx<T>* buf, int t,
-                                              const cplx<T>* __restrict__ tw, int tws) {
+                                              const cplx<T>* __restrict__ stw) {
+  constexpr int R = PE<N, E>::radix(S);
+  constexpr bool LAST = S == PE<N, E>::NST - 1;
+  stageE_st<T, R, E, INV>(v, buf, t, PE<N, E>::T, NS, stw + (S > 0 ? PE<N, E>::twoff(S) : 0),
+                          LAST);
+  if constexpr (!LAST) {
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = buf[pad16(t + PE<N, E>::T * q)];
+    __syncthreads();
+    fftE_ct_stage<T, N, E, INV, S + 1, NS * R>(v, buf, t, stw);
+  }
+}
+
+// Transform one line held as v[q] = x[t + (N/E) q] (see fft8_line), with
+// the per-stage twiddle table `stw` of PE<N, E> (fftE_ct_twiddles).
+template <typename T, int N, int E, bool INV>
+__device__ __forceinline__ void fftE_ct(cplx<T> (&v)[E], cplx<T>* buf, int t,
+                                        const cplx<T>* __restrict__ stw) {
+  fftE_ct_stage<T, N, E, INV, 0, 1>(v, buf, t, stw);
+}
+
+// The same transform reading the natural table `tw` with stride tws.
+template <typename T, int N, int E, bool INV, int S, int NS>
+__device__ __forceinline__ void fftE_ct_stage_nat(cplx<T> (&v)[E], cplx<T>* buf, int t,
+                                                  const cplx<T>* __restrict__ tw, int tws) {
   constexpr int R = PE<N, E>::radix(S);
   constexpr bool LAST = S == PE<N, E>::NST - 1;
   stageE<T, R, E, INV>(v, buf, t, PE<N, E>::T, NS, N, tw, tws, LAST);
@@ -44,21 +141,16 @@ __device__ __forceinline__ void fftE_ct_stage(cplx<T> (&v)[E], cplx<T>* buf, int
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = buf[pad16(t + PE<N, E>::T * q)];
     __syncthreads();
-    fftE_ct_stage<T, N, E, INV, S + 1, NS * R>(v, buf, t, tw, tws);
+    fftE_ct_stage_nat<T, N, E, INV, S + 1, NS * R>(v, buf, t, tw, tws);
   }
 }
 
-// Transform one line held as v[q] = x[t + (N/E) q] (see fft8_line).
 template <typename T, int N, int E, bool INV>
-__device__ __forceinline__ void fftE_ct(cplx<T> (&v)[E], cplx<T>* buf, int t,
-                                        const cplx<T>* __restrict__ tw, int tws) {
-  fftE_ct_stage<T, N, E, INV, 0, 1>(v, buf, t, tw, tws);
+__device__ __forceinline__ void fftE_ct_nat(cplx<T> (&v)[E], cplx<T>* buf, int t,
+                                            const cplx<T>* __restrict__ tw, int tws) {
+  fftE_ct_stage_nat<T, N, E, INV, 0, 1>(v, buf, t, tw, tws);
 }
 
-template <typename T, int N, bool INV>
-__device__ __forceinline__ void fft8_ct(cplx<T> (&v)[8], cplx<T>* buf, int t,
-                                        const cplx<T>* __restrict__ tw, int tws) {
-  fftE_ct<T, N, 8, INV>(v, buf, t, tw, tws);
-}
+
 
 }  // namespace bri17gb

@@ -82,7 +82,7 @@ bool ct_rows_c2r(int m, const cplx<T>* X, typename IoOf<T>::type* x, int64_t nro
     const int TT = N / E;                                                             \
     const int rb = ct_rows_per_cta(TT, nrows, mask);                                  \
     const int pitch = exchange_pitch(N, rb, (int)sizeof(cplx<T>), false);             \
-    const size_t smem = (2 * N + (size_t)rb * pitch) * sizeof(cplx<T>);               \
+    const size_t smem = (3 * N + (size_t)rb * pitch) * sizeof(cplx<T>);               \
     launch_pdl(rows_c2r_p2<T, CtEng<N, E>>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st,  \
         X, x, nrows, H, CtEng<N, E>{}, tw, rb, pitch, mask);                          \
     return true;                                                                      \

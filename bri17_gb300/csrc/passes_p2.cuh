@@ -4,6 +4,8 @@
 // serving every other length.
 #pragma once
 
+#include <type_traits>
+
 #include "df64.cuh"
 #include "fft8.cuh"
 #include "fft8_ct.cuh"
@@ -15,11 +17,27 @@ namespace bri17gb {
 
 // Engine policies: the kernels below take either the runtime-plan engine
 // (any power-of-two length) or a compile-time-length engine.
+// load_tw fills the kernel's shared twiddle table from the natural global
+// table (`count` entries read with stride `tws` by the transform); run then
+// takes that shared table.  The runtime engine copies the natural table;
+// the compile-time engine lays out per-stage tables (fftE_ct_twiddles), so
+// consecutive butterflies read consecutive entries -- except in float pairs,
+// whose transforms are bound by arithmetic, not by shared-memory banks, and
+// keep the cheaper natural copy.  stage<S>() tells which table run reads.
 struct RtEng {
   static constexpr int E = 8;
+  template <typename S>
+  static constexpr bool stage() {
+    return false;
+  }
   Plan8 p;
   __device__ __forceinline__ int n() const { return p.n; }
   __device__ __forceinline__ int T() const { return p.T; }
+  template <typename S>
+  __device__ __forceinline__ void load_tw(cplx<S>* dst, const cplx<S>* __restrict__ src,
+                                          int count, int tws) const {
+    for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = src[i];
+  }
   template <typename S, bool INV>
   __device__ __forceinline__ void run(cplx<S> (&v)[8], cplx<S>* buf, int t,
                                       const cplx<S>* __restrict__ tw, int tws) const {
@@ -30,12 +48,27 @@ struct RtEng {
 template <int N, int EE = 8>
 struct CtEng {
   static constexpr int E = EE;
+  template <typename S>
+  static constexpr bool stage() {
+    return !std::is_same<S, df64>::value;
+  }
   __device__ __forceinline__ constexpr int n() const { return N; }
   __device__ __forceinline__ constexpr int T() const { return N / EE; }
+  template <typename S>
+  __device__ __forceinline__ void load_tw(cplx<S>* dst, const cplx<S>* __restrict__ src,
+                                          int count, int tws) const {
+    if constexpr (stage<S>())
+      fftE_ct_twiddles<S, N, EE>(dst, src, tws, threadIdx.x, blockDim.x);
+    else
+      for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = src[i];
+  }
   template <typename S, bool INV>
   __device__ __forceinline__ void run(cplx<S> (&v)[EE], cplx<S>* buf, int t,
                                       const cplx<S>* __restrict__ tw, int tws) const {
-    fftE_ct<S, N, EE, INV>(v, buf, t, tw, tws);
+    if constexpr (stage<S>())
+      fftE_ct<S, N, EE, INV>(v, buf, t, tw);
+    else
+      fftE_ct_nat<S, N, EE, INV>(v, buf, t, tw, tws);
   }
 };
 
@@ -60,10 +93,10 @@ __global__ void __launch_bounds__(kP2Threads)
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
   pdl_launch_dependents();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  pm.template load_tw<T>(tw, tw_g, n, 2);
+  for (int i = threadIdx.x; i <= m; i += blockDim.x) {
     const cplx<T> w = tw_g[i];
-    tw[i] = w;
-    if (i <= m) twh[i] = mk<T>(T(0.5) * w.x, T(0.5) * w.y);
+    twh[i] = mk<T>(T(0.5) * w.x, T(0.5) * w.y);
   }
   pdl_wait();
   if (mask.skip(row0)) return;
@@ -111,14 +144,18 @@ __global__ void __launch_bounds__(kP2Threads)
   using Io = typename IoOf<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = pm.n(), n = 2 * m, TT = pm.T();
+  // Natural table (the split step reads W^k) and, for the compile-time
+  // engine, the transform's per-stage tables after it.
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* bufs = tw + n;
+  cplx<T>* stw = tw + n;
+  cplx<T>* bufs = stw + (Eng::template stage<T>() ? m : 0);
   const int64_t row0 = (int64_t)blockIdx.x * RB;
   const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
   pdl_launch_dependents();
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  if constexpr (Eng::template stage<T>()) pm.template load_tw<T>(stw, tw_g, n, 2);
   __syncthreads();
   pdl_wait();
   if (mask.skip(row0)) return;
@@ -138,7 +175,7 @@ __global__ void __launch_bounds__(kP2Threads)
       v[q] = mk<T>(T(0), T(0));
     }
   }
-  pm.template run<T, true>(v, bufs + rb * pitch, t, tw, 2);
+  pm.template run<T, true>(v, bufs + rb * pitch, t, Eng::template stage<T>() ? stw : tw, 2);
   if (!valid) return;
   cplx<Io>* xc = reinterpret_cast<cplx<Io>*>(x) + row * m;
 #pragma unroll
@@ -160,7 +197,7 @@ __global__ void __launch_bounds__(kP2Threads)
   const bool valid = b < B;
   cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b;
   pdl_launch_dependents();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+  p.template load_tw<T>(tw, tw_g, n, 1);
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
   cplx<T> v[Eng::E];
@@ -252,7 +289,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   const bool valid = b < P;
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
   pdl_launch_dependents();
-  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
   T s = fp.s, mu = fp.mu;
@@ -340,7 +377,7 @@ __global__ void __launch_bounds__(kP2Threads)
   const bool valid = b < P;
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
   pdl_launch_dependents();
-  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
   T s = fp.s, mu = fp.mu;
@@ -441,7 +478,7 @@ __global__ void __launch_bounds__(256)
   const int z = blockIdx.y;
   pdl_launch_dependents();
   if (threadIdx.x == 0) mbar_init(bar, 1);
-  for (int i = threadIdx.x; i < n0; i += blockDim.x) tw[i] = fp.tab.tw[0][i];
+  p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
   // The copy destinations must be 128-byte aligned; the launch guarantees
