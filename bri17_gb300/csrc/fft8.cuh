@@ -52,14 +52,14 @@ __device__ __forceinline__ int pad16(int p) { return p + (p >> 4); }
 __host__ __device__ __forceinline__ int pitch8(int n) { return n + n / 16 + 1; }
 
 // Pitch (complex elements) of the exchange buffers of `lines` lines of
-// length n (a power of two, 8..1024) held by one CTA with the eight-element
-// engine, for elements of csize bytes.  lines_fastest: consecutive threads
+// length n (a power of two, 8..1024) held by one CTA with the E-element
+// engine (8 or 16 elements per thread), for elements of csize bytes.  lines_fastest: consecutive threads
 // step across the lines first (thread = t * lines + line, the strided-axis
 // passes); otherwise along a line first (thread = line * (n/8) + t, the row
 // passes).  Chosen among n + n/16 + {0..15} by a model of the exchanges'
 // shared-memory wavefronts (every stage's scattered writes and strided
 // reads, 32 banks of 4 bytes); cached per argument set (host, thread-safe).
-int exchange_pitch(int n, int lines, int csize, bool lines_fastest);
+int exchange_pitch(int n, int lines, int csize, bool lines_fastest, int E = 8);
 
 // Pitch of lines accessed only in natural order with warp lanes stepping
 // across the TB lines first: lines stagger by 32 / TB elements modulo the M

@@ -316,7 +316,34 @@ int access_wavefronts(const int* byte_addr, int lanes, int csize) {
   return best;
 }
 
-long exchange_wavefronts(const Plan8& p, int lines, int pitch, int csize, bool lines_fastest) {
+// Stage schedule of the engines: E = 8 as make_plan8 (8s, then 4 x 4 or
+// 4); E = 16 as the compile-time engine's (16s, then one stage of the
+// remaining power of two).
+struct StagePlan {
+  int T, nst, radix[12];
+};
+
+bool stage_plan(int n, int E, StagePlan* sp) {
+  if (E == 8) {
+    Plan8 p;
+    if (!make_plan8(n, &p)) return false;
+    sp->T = p.T;
+    sp->nst = p.nst;
+    for (int s = 0; s < p.nst; s++) sp->radix[s] = p.radix[s];
+    return true;
+  }
+  if (E != 16 || !is_pow2(n) || n < 16 || n > 1024) return false;
+  int ln = 0;
+  while ((1 << ln) < n) ln++;
+  sp->T = n / 16;
+  sp->nst = 0;
+  for (int s = 0; s < ln / 4; s++) sp->radix[sp->nst++] = 16;
+  if (ln % 4) sp->radix[sp->nst++] = 1 << (ln % 4);
+  return true;
+}
+
+long exchange_wavefronts(const StagePlan& p, int E, int lines, int pitch, int csize,
+                         bool lines_fastest) {
   const int T = p.T;
   const int nthreads = T * lines;
   long total = 0;
@@ -326,7 +353,7 @@ long exchange_wavefronts(const Plan8& p, int lines, int pitch, int csize, bool l
     const int lanes = std::min(32, nthreads - w0);
     int Ns = 1;
     for (int s = 0; s + 1 < p.nst; s++) {
-      const int R = p.radix[s], M = 8 / R;
+      const int R = p.radix[s], M = E / R;
       for (int m = 0; m < M; m++)
         for (int r = 0; r < R; r++) {
           for (int l = 0; l < lanes; l++) {
@@ -338,7 +365,7 @@ long exchange_wavefronts(const Plan8& p, int lines, int pitch, int csize, bool l
           }
           total += access_wavefronts(addr, lanes, csize);
         }
-      for (int q = 0; q < 8; q++) {
+      for (int q = 0; q < E; q++) {
         for (int l = 0; l < lanes; l++) {
           const int tid = w0 + l;
           const int line = lines_fastest ? tid % lines : tid / T;
@@ -355,20 +382,21 @@ long exchange_wavefronts(const Plan8& p, int lines, int pitch, int csize, bool l
 
 }  // namespace
 
-int exchange_pitch(int n, int lines, int csize, bool lines_fastest) {
+int exchange_pitch(int n, int lines, int csize, bool lines_fastest, int E) {
   static std::mutex mu;
   static std::map<long, int> cache;
-  const long key = (((long)n * 4096 + lines) * 64 + csize) * 2 + (lines_fastest ? 1 : 0);
+  const long key =
+      ((((long)n * 4096 + lines) * 64 + csize) * 2 + (lines_fastest ? 1 : 0)) * 32 + E;
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
-  Plan8 p;
+  StagePlan p;
   int best = pitch8(n);
-  if (make_plan8(n, &p) && lines >= 1) {
+  if (stage_plan(n, E, &p) && lines >= 1) {
     long best_w = -1;
     for (int d = 0; d < 16; d++) {
       const int pitch = n + n / 16 + d;
-      const long w = exchange_wavefronts(p, lines, pitch, csize, lines_fastest);
+      const long w = exchange_wavefronts(p, E, lines, pitch, csize, lines_fastest);
       if (best_w < 0 || w < best_w) {
         best_w = w;
         best = pitch;

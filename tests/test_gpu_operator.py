@@ -74,6 +74,8 @@ SHAPES = [
     ((8, 16, 16), (1.0, 1.0, 1.0), 1.0, 0.3),
     ((256, 64, 128), (1.0, 0.25, 0.5), 1.0, 0.3),
     ((1, 6, 10), (1.0, 1.0, 1.0), 1.0, 0.3),    # degenerate first axis
+    ((8, 256, 64), (1.0, 2.0, 0.5), 1.0, 0.3),   # axis-1 lengths of the 16-element FP32 pass
+    ((4, 512, 32), (1.0, 1.0, 1.0), 0.8, 0.2),
 ]
 
 
