@@ -617,9 +617,16 @@ def run_serve(args):
     # for 512 requests; a generator thread alone produces them slower than
     # the arrival rate, which would throttle the stream).  numpy releases the
     # GIL while filling, so a thread pool spreads the work over the cores.
+    # They are generated into page-locked buffers (a server's receive
+    # buffers), which the server borrows without a copy.
     from concurrent.futures import ThreadPoolExecutor
+
+    def make_pinned(r):
+        t = torch.empty((6,) + (r["side"],) * 3, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = make_tau(r)
+        return t
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
-        taus = list(ex.map(make_tau, reqs))
+        taus = list(ex.map(make_pinned, reqs))
     srv = Server(memory_budget_bytes=args.memory_gb << 30, slots_per_bucket=args.slots)
     # Warm the buckets (graph capture, first-touch) with one tiny solve per size.
     for s in (32, 48, 64, 96, 128):

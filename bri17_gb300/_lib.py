@@ -85,6 +85,8 @@ _SIGS = {
     "bri17_server_destroy": ([vp], ctypes.c_int),
     "bri17_server_submit": ([vp, c_int_p, c_double_p, ctypes.c_double, ctypes.c_double,
                              vp, vp, ctypes.c_double, ctypes.c_int, c_int64_p], ctypes.c_int),
+    "bri17_server_submit_borrowed": ([vp, c_int_p, c_double_p, ctypes.c_double, ctypes.c_double,
+                             vp, vp, ctypes.c_double, ctypes.c_int, c_int64_p], ctypes.c_int),
     "bri17_server_step": ([vp, c_int_p], ctypes.c_int),
     "bri17_server_poll": ([vp, ctypes.POINTER(RequestResult), ctypes.c_int, c_int_p],
                           ctypes.c_int),

@@ -48,8 +48,12 @@ struct Request {
   int shape[3];
   double L[3];
   double mu, nu;
-  std::vector<double> tau;  // 6 x size
+  std::vector<double> tau;  // 6 x size (copied at submit)
+  const double* tau_borrowed = nullptr;  // or the caller's buffer (borrowed submit)
   double* x_host;
+  bool x_locked = false;   // x_host is page-locked: the result copy is asynchronous
+  cudaEvent_t done_ev = nullptr;  // that copy's completion
+  int final_status = BRI17_OK;
   double tol;
   int max_iterations;
   double t_submit = 0, t_admit = 0, t_finish = 0;
@@ -326,6 +330,7 @@ struct bri17_server {
   std::vector<Bucket*> buckets;
   std::vector<bri17_request_result> done;
   std::unordered_map<int64_t, Request*> live;
+  std::vector<Request*> finishing;  // solution copies to page-locked x_host in flight
   std::chrono::steady_clock::time_point t0;
   double now() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -525,6 +530,7 @@ void finish(bri17_server* srv, Request* q, int status) {
   res.finish_time_s = q->t_finish;
   srv->done.push_back(res);
   srv->live.erase(q->id);
+  if (q->done_ev) cudaEventDestroy(q->done_ev);
   delete q;
 }
 
@@ -537,7 +543,8 @@ int admit(bri17_server* srv, Bucket* B, int z, Request* q) {
   q->t_admit = srv->now();
   // The slot stays masked out of the chunks until its first outer decision.
   ks_set_inactive<<<1, 1, 0, s>>>(B->st + z);
-  SRV_TRY(cudaMemcpyAsync(B->tau, q->tau.data(), 6 * B->size * 8, cudaMemcpyHostToDevice, s));
+  SRV_TRY(cudaMemcpyAsync(B->tau, q->tau_borrowed ? q->tau_borrowed : q->tau.data(),
+                          6 * B->size * 8, cudaMemcpyHostToDevice, s));
   const double corr = B->op64->corr;
   const double scaling = q->mu / (1. - 2. * q->nu);
   q->mat64[0] = scaling * corr;
@@ -580,13 +587,24 @@ int outer_decide(bri17_server* srv, Bucket* B, int z, bool* busy) {
   const bool converged = q->rel <= q->tol || q->bb == 0.0;
   if (converged || q->iters >= q->max_iterations || q->cancel) {
     const int64_t n = B->n;
+    const int status = q->cancel ? BRI17_ERR_CANCELLED
+                                 : converged ? BRI17_OK : BRI17_ERR_NOT_CONVERGED;
     SRV_TRY(cudaMemcpyAsync(q->x_host, B->x + z * n, n * 8, cudaMemcpyDeviceToHost,
                             B->stream));
-    SRV_TRY(cudaStreamSynchronize(B->stream));
     B->slot_state[z] = kFree;
     B->slot_req[z] = nullptr;
-    finish(srv, q, q->cancel ? BRI17_ERR_CANCELLED
-                             : converged ? BRI17_OK : BRI17_ERR_NOT_CONVERGED);
+    if (q->x_locked) {
+      // The copy runs on the bucket's stream (later work in the slot waits
+      // for it); the request finishes when the step sees its event.
+      SRV_TRY(cudaEventCreateWithFlags(&q->done_ev, cudaEventDisableTiming));
+      SRV_TRY(cudaEventRecord(q->done_ev, B->stream));
+      q->final_status = status;
+      srv->finishing.push_back(q);
+      B->enqueued = true;
+      return BRI17_OK;
+    }
+    SRV_TRY(cudaStreamSynchronize(B->stream));
+    finish(srv, q, status);
     return BRI17_OK;
   }
   const int64_t n = B->n;
@@ -635,6 +653,8 @@ extern "C" int bri17_server_create(int64_t budget, int max_active, bri17_server*
 extern "C" int bri17_server_destroy(bri17_server* srv) {
   if (!srv) return BRI17_OK;
   for (Bucket* B : srv->buckets) free_bucket(B);
+  for (Request* q : srv->finishing)
+    if (q->done_ev) cudaEventDestroy(q->done_ev);
   for (Request* q : srv->queue) delete q;
   for (auto& kv : srv->live)
     if (std::find(srv->queue.begin(), srv->queue.end(), kv.second) == srv->queue.end())
@@ -643,10 +663,20 @@ extern "C" int bri17_server_destroy(bri17_server* srv) {
   return BRI17_OK;
 }
 
-extern "C" int bri17_server_submit(bri17_server* srv, const int* shape, const double* L,
-                                   double mu, double nu, const double* tau_host,
-                                   double* x_host, double tol, int max_iterations,
-                                   int64_t* id) {
+namespace {
+
+bool page_locked(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+int submit_request(bri17_server* srv, const int* shape, const double* L, double mu, double nu,
+                   const double* tau_host, double* x_host, double tol, int max_iterations,
+                   bool borrow, int64_t* id) {
   if (!srv || !shape || !L || !tau_host || !x_host || !id) {
     set_error("null pointer");
     return BRI17_ERR_INVALID_ARGUMENT;
@@ -677,8 +707,12 @@ extern "C" int bri17_server_submit(bri17_server* srv, const int* shape, const do
   q->mu = mu;
   q->nu = nu;
   const int64_t size = (int64_t)shape[0] * shape[1] * shape[2];
-  q->tau.assign(tau_host, tau_host + 6 * size);
+  if (borrow)
+    q->tau_borrowed = tau_host;
+  else
+    q->tau.assign(tau_host, tau_host + 6 * size);
   q->x_host = x_host;
+  q->x_locked = page_locked(x_host);
   q->tol = tol;
   q->max_iterations = max_iterations;
   q->t_submit = srv->now();
@@ -686,6 +720,24 @@ extern "C" int bri17_server_submit(bri17_server* srv, const int* shape, const do
   srv->live[q->id] = q;
   *id = q->id;
   return BRI17_OK;
+}
+
+}  // namespace
+
+extern "C" int bri17_server_submit(bri17_server* srv, const int* shape, const double* L,
+                                   double mu, double nu, const double* tau_host,
+                                   double* x_host, double tol, int max_iterations,
+                                   int64_t* id) {
+  return submit_request(srv, shape, L, mu, nu, tau_host, x_host, tol, max_iterations, false,
+                        id);
+}
+
+extern "C" int bri17_server_submit_borrowed(bri17_server* srv, const int* shape,
+                                            const double* L, double mu, double nu,
+                                            const double* tau_host, double* x_host,
+                                            double tol, int max_iterations, int64_t* id) {
+  return submit_request(srv, shape, L, mu, nu, tau_host, x_host, tol, max_iterations, true,
+                        id);
 }
 
 extern "C" int bri17_server_cancel(bri17_server* srv, int64_t id) {
@@ -776,6 +828,19 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
     return BRI17_ERR_INVALID_ARGUMENT;
   }
   bool progress = false;
+  // 0. Requests whose solution copy to a page-locked buffer has completed.
+  for (size_t i = 0; i < srv->finishing.size();) {
+    Request* q = srv->finishing[i];
+    const cudaError_t qs = cudaEventQuery(q->done_ev);
+    if (qs == cudaErrorNotReady) {
+      i++;
+      continue;
+    }
+    if (qs != cudaSuccess) return cuda_fail(qs, "server result copy");
+    srv->finishing.erase(srv->finishing.begin() + i);
+    finish(srv, q, q->final_status);
+    progress = true;
+  }
   // 1. Retire completed chunks.
   for (Bucket* B : srv->buckets) {
     if (!B->in_flight) continue;
@@ -847,6 +912,8 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
     while (!any && std::chrono::steady_clock::now() < t_end) {
       for (Bucket* B : srv->buckets)
         if (B->in_flight && cudaStreamQuery(B->stream) != cudaErrorNotReady) any = true;
+      for (Request* q : srv->finishing)
+        if (cudaEventQuery(q->done_ev) != cudaErrorNotReady) any = true;
       if (!any) std::this_thread::sleep_for(std::chrono::microseconds(10));
     }
   }

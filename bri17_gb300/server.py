@@ -18,6 +18,15 @@ from . import _lib
 from ._lib import check
 
 
+def _pinned_torch():
+    """torch when page-locked host memory is available, else None."""
+    try:
+        import torch
+    except ImportError:
+        return None
+    return torch if torch.cuda.is_available() else None
+
+
 class Server:
     def __init__(self, memory_budget_bytes: int = 8 << 30, slots_per_bucket: int = 64):
         L = _lib.load()
@@ -44,19 +53,44 @@ class Server:
         return _lib.load().bri17_server_clock(self._h)
 
     def submit(self, shape, L, mu, nu, tau, tol=1e-8, max_iterations=100000) -> int:
+        """Queue one solve.  tau (numpy array or CPU tensor, (6, *shape)) is
+        copied into page-locked memory held until the request is polled -- a
+        page-locked float64 tensor is borrowed without a copy -- and the
+        solution lands in a page-locked array, so the server's uploads and
+        downloads are asynchronous (bri17_server_submit_borrowed)."""
         shape = tuple(int(n) for n in shape)
         if len(shape) != 3:
             raise ValueError("the server solves 3D problems")
-        tau = np.ascontiguousarray(tau, dtype=np.float64)
-        if tau.size != 6 * int(np.prod(shape)):
+        torch = _pinned_torch()
+        if torch is not None and isinstance(tau, torch.Tensor):
+            # A page-locked float64 CPU tensor is borrowed as it is.
+            if tau.is_cuda:
+                raise ValueError("tau must be host memory")
+            tau = tau if (tau.dtype == torch.float64 and tau.is_contiguous()
+                          and tau.is_pinned()) else tau.to(torch.float64).contiguous().numpy()
+        else:
+            tau = np.ascontiguousarray(tau, dtype=np.float64)
+        count = tau.size if isinstance(tau, np.ndarray) else tau.numel()
+        if count != 6 * int(np.prod(shape)):
             raise ValueError("tau must hold 6 x prod(shape) values")
-        x = np.zeros((3,) + shape)
         rid = ctypes.c_int64()
-        check(_lib.load().bri17_server_submit(
-            self._h, (ctypes.c_int * 3)(*shape), (ctypes.c_double * 3)(*L), float(mu),
-            float(nu), tau.ctypes.data_as(ctypes.c_void_p), x.ctypes.data_as(ctypes.c_void_p),
-            float(tol), int(max_iterations), ctypes.byref(rid)), "bri17_server_submit")
-        self._out[rid.value] = x
+        args = ((ctypes.c_int * 3)(*shape), (ctypes.c_double * 3)(*L), float(mu), float(nu))
+        if torch is not None:
+            tau_t = tau if isinstance(tau, torch.Tensor) else torch.from_numpy(tau).pin_memory()
+            x_t = torch.zeros((3,) + shape, dtype=torch.float64, pin_memory=True)
+            check(_lib.load().bri17_server_submit_borrowed(
+                self._h, *args, ctypes.c_void_p(tau_t.data_ptr()),
+                ctypes.c_void_p(x_t.data_ptr()), float(tol), int(max_iterations),
+                ctypes.byref(rid)), "bri17_server_submit_borrowed")
+            self._taus[rid.value] = tau_t
+            self._out[rid.value] = (x_t, x_t.numpy())
+        else:
+            x = np.zeros((3,) + shape)
+            check(_lib.load().bri17_server_submit(
+                self._h, *args, tau.ctypes.data_as(ctypes.c_void_p),
+                x.ctypes.data_as(ctypes.c_void_p), float(tol), int(max_iterations),
+                ctypes.byref(rid)), "bri17_server_submit")
+            self._out[rid.value] = (None, x)
         self.pending += 1
         return rid.value
 
@@ -78,10 +112,12 @@ class Server:
                         "rel_residual": r.rel_residual, "submit_time_s": r.submit_time_s,
                         "admit_time_s": r.admit_time_s, "finish_time_s": r.finish_time_s})
         self.pending -= len(out)
+        for r in out:
+            self._taus.pop(r["id"], None)  # borrowed until the request is returned
         return out
 
     def result(self, rid: int) -> np.ndarray:
-        return self._out.pop(rid)
+        return self._out.pop(rid)[1]
 
     def cancel(self, rid: int) -> int:
         return _lib.load().bri17_server_cancel(self._h, int(rid))

@@ -327,6 +327,20 @@ int bri17_server_submit(bri17_server* srv, const int* shape, const double* L,
                         double* x_host, double tol, int max_iterations,
                         int64_t* id);
 
+/*
+ * Same, without the copy of tau at submit: tau_host is read when the request
+ * is admitted and must stay valid and unchanged until bri17_server_poll
+ * returns the request.  With page-locked tau_host and x_host (cudaHostAlloc,
+ * cudaHostRegister) the upload and the solution's download are asynchronous
+ * copies, so admissions and retirements never block the server's step.
+ * (bri17_server_submit also downloads asynchronously into a page-locked
+ * x_host.)
+ */
+int bri17_server_submit_borrowed(bri17_server* srv, const int* shape,
+                                 const double* L, double mu, double nu,
+                                 const double* tau_host, double* x_host,
+                                 double tol, int max_iterations, int64_t* id);
+
 /* Advance the server: admit, run one scheduling quantum, retire.  Returns
  * the number of active requests in *active. */
 int bri17_server_step(bri17_server* srv, int* active);
