@@ -627,46 +627,66 @@ def run_serve(args):
         return t
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         taus = list(ex.map(make_pinned, reqs))
-    srv = Server(memory_budget_bytes=args.memory_gb << 30, slots_per_bucket=args.slots)
-    # Warm the buckets (graph capture, first-touch) with one tiny solve per size.
-    for s in (32, 48, 64, 96, 128):
-        srv.submit((s, s, s), (1, 1, 1), 1.0, 0.3, np.zeros((6, s, s, s)), tol=1e-8)
-    srv.run_until_idle()
-    sampler = ClockSampler(0)
-    sampler.start()
-    t_start = srv.clock()
-    submitted, done = 0, {}
-    meta = {}
-    host_s = {"submit": 0.0, "step": 0.0, "steps": 0}
-    while len(done) < nreq:
-        now = srv.clock() - t_start
-        while submitted < nreq:
-            r, tau = reqs[submitted], taus[submitted]
-            if r["t"] > now:
-                break
-            s = r["side"]
-            h0 = time.perf_counter()
-            rid = srv.submit((s, s, s), (1, 1, 1), r["mu"], r["nu"], tau, tol=1e-8)
-            host_s["submit"] += time.perf_counter() - h0
-            meta[rid] = r
-            taus[submitted] = None
-            submitted += 1
-        if srv.pending:
-            h0 = time.perf_counter()
-            srv.step()
-            host_s["step"] += time.perf_counter() - h0
-            host_s["steps"] += 1
-            for res in srv.poll():
-                if res["id"] in meta:
-                    done[res["id"]] = res
-                srv.result(res["id"])
-        else:
-            time.sleep(0.0005)
-    makespan = max(d["finish_time_s"] for d in done.values()) - t_start
-    clocks = sampler.stop()
-    lat = np.array([done[i]["finish_time_s"] - t_start - meta[i]["t"] for i in done])
-    ok = sum(1 for d in done.values() if d["status"] == 0)
-    srv.close()
+    def stream(size_priority, taus):
+        """One pass of the request stream through a fresh server; taus are
+        consumed (dropped once submitted)."""
+        srv = Server(memory_budget_bytes=args.memory_gb << 30, slots_per_bucket=args.slots,
+                     size_priority=size_priority)
+        # Warm the buckets (graph capture, first-touch) with one tiny solve per size.
+        for s in (32, 48, 64, 96, 128):
+            srv.submit((s, s, s), (1, 1, 1), 1.0, 0.3, np.zeros((6, s, s, s)), tol=1e-8)
+        srv.run_until_idle()
+        sampler = ClockSampler(0)
+        sampler.start()
+        t_start = srv.clock()
+        submitted, done = 0, {}
+        meta = {}
+        host_s = {"submit": 0.0, "step": 0.0, "steps": 0}
+        while len(done) < nreq:
+            now = srv.clock() - t_start
+            while submitted < nreq:
+                r, tau = reqs[submitted], taus[submitted]
+                if r["t"] > now:
+                    break
+                s = r["side"]
+                h0 = time.perf_counter()
+                rid = srv.submit((s, s, s), (1, 1, 1), r["mu"], r["nu"], tau, tol=1e-8)
+                host_s["submit"] += time.perf_counter() - h0
+                meta[rid] = r
+                taus[submitted] = None
+                submitted += 1
+            if srv.pending:
+                h0 = time.perf_counter()
+                srv.step()
+                host_s["step"] += time.perf_counter() - h0
+                host_s["steps"] += 1
+                for res in srv.poll():
+                    if res["id"] in meta:
+                        done[res["id"]] = res
+                    srv.result(res["id"])
+            else:
+                time.sleep(0.0005)
+        makespan = max(d["finish_time_s"] for d in done.values()) - t_start
+        clocks = sampler.stop()
+        lat = np.array([done[i]["finish_time_s"] - t_start - meta[i]["t"] for i in done])
+        ok = sum(1 for d in done.values() if d["status"] == 0)
+        srv.close()
+        ids = list(done)
+        stats = {"solves_per_s": nreq / makespan, "makespan_s": makespan,
+                 "p50_latency_s": float(np.percentile(lat, 50)),
+                 "p99_latency_s": float(np.percentile(lat, 99)), "succeeded": ok,
+                 "p50_latency_s_per_size": {
+                     str(sz): float(np.percentile(
+                         [lat[j] for j, i in enumerate(ids) if meta[i]["side"] == sz], 50))
+                     for sz in (32, 48, 64, 96, 128)},
+                 "host_time_s": host_s}
+        return stats, clocks
+
+    # The second pass re-reads the same page-locked inputs (borrowed, unchanged).
+    taus_prio = list(taus) if args.serve_priority_run else None
+    main_stats, clocks = stream(False, taus)
+    prio_stats = stream(True, taus_prio)[0] if taus_prio is not None else None
+    makespan = main_stats["makespan_s"]
 
     # One-at-a-time FP64 baseline on a subsample (2 per size), then a FIFO
     # single-server queue over the same arrivals with per-size service times.
@@ -705,15 +725,8 @@ def run_serve(args):
                                "mean 5 ms, cubic sides {32,48,64,96,128}, mu~U[0.5,2], "
                                "nu~U[0.1,0.45], tau~N(0,1), tol 1e-8, seed 3",
                    "slots_per_bucket": args.slots, "memory_budget_gb": args.memory_gb},
-        "batched_mixed": {"solves_per_s": nreq / makespan, "makespan_s": makespan,
-                          "p50_latency_s": float(np.percentile(lat, 50)),
-                          "p99_latency_s": float(np.percentile(lat, 99)),
-                          "succeeded": ok,
-                          "p50_latency_s_per_size": {
-                              str(sz): float(np.percentile(
-                                  [lat[j] for j, i in enumerate(done) if meta[i]["side"] == sz],
-                                  50)) for sz in (32, 48, 64, 96, 128)},
-                          "host_time_s": host_s},
+        "batched_mixed": main_stats,
+        "batched_mixed_size_priority": prio_stats,
         "one_at_a_time_fp64": {"solves_per_s": nreq / base_makespan,
                                "makespan_s": base_makespan,
                                "p50_latency_s": float(np.percentile(lat_b, 50)),
@@ -733,6 +746,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--no-serve-priority-run", dest="serve_priority_run",
+                    action="store_false",
+                    help="--workload serve: skip the second pass with size priorities")
     ap.add_argument("--cg-reps", type=int, default=0,
                     help="timed solves per mode for --workload cg / aniso "
                          "(default 3 mixed, 1 plain)")

@@ -83,6 +83,7 @@ _SIGS = {
                         ctypes.POINTER(CgInfo), vp], ctypes.c_int),
     "bri17_server_create": ([ctypes.c_int64, ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
     "bri17_server_destroy": ([vp], ctypes.c_int),
+    "bri17_server_set_size_priority": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_server_submit": ([vp, c_int_p, c_double_p, ctypes.c_double, ctypes.c_double,
                              vp, vp, ctypes.c_double, ctypes.c_int, c_int64_p], ctypes.c_int),
     "bri17_server_submit_borrowed": ([vp, c_int_p, c_double_p, ctypes.c_double, ctypes.c_double,

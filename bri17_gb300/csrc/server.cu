@@ -25,6 +25,8 @@
 // Admission is by device footprint: a new bucket is created only while the
 // server's total allocation stays within its memory budget.
 #include <math.h>
+
+#include <cmath>
 #include <string.h>
 
 #include <algorithm>
@@ -324,6 +326,7 @@ using namespace bri17gb;
 struct bri17_server {
   int64_t budget = 0;
   int max_active = 8;  // most slots per bucket
+  bool size_priority = false;  // smaller geometries' streams first
   int64_t used = 0;
   int64_t next_id = 1;
   std::deque<Request*> queue;
@@ -461,7 +464,17 @@ int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
       cudaMemset(B->mat64, 0, S * 2 * 8) != cudaSuccess ||
       cudaMemset(B->p32, 0, Sn * 4) != cudaSuccess)
     return fail(cuda_fail(cudaErrorUnknown, "cudaMemset(bucket)"));
-  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
+  // With size priorities on, smaller geometries get higher stream priority:
+  // their short kernels are scheduled ahead of the queued CTAs of large
+  // buckets' passes (lower latency for small requests, lower throughput).
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  const int levels = least - greatest + 1;
+  const double tpos = std::max(0.0, std::log2((double)B->size / 32768.0)) / 6.0;
+  const int prio = srv->size_priority
+                       ? greatest + std::min(levels - 1, (int)std::lround(tpos * (levels - 1)))
+                       : least;
+  if (cudaStreamCreateWithPriority(&B->stream, cudaStreamNonBlocking, prio) != cudaSuccess)
     return fail(cuda_fail(cudaErrorUnknown, "cudaStreamCreate"));
   B->slot_state.assign(S, kFree);
   B->slot_req.assign(S, nullptr);
@@ -647,6 +660,15 @@ extern "C" int bri17_server_create(int64_t budget, int max_active, bri17_server*
   s->max_active = max_active;
   s->t0 = std::chrono::steady_clock::now();
   *out = s;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_server_set_size_priority(bri17_server* srv, int enable) {
+  if (!srv) {
+    set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  srv->size_priority = enable != 0;
   return BRI17_OK;
 }
 

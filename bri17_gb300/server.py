@@ -28,12 +28,17 @@ def _pinned_torch():
 
 
 class Server:
-    def __init__(self, memory_budget_bytes: int = 8 << 30, slots_per_bucket: int = 64):
+    def __init__(self, memory_budget_bytes: int = 8 << 30, slots_per_bucket: int = 64,
+                 size_priority: bool = False):
+        """size_priority: smaller geometries on higher-priority streams (lower
+        latency for small requests, lower throughput)."""
         L = _lib.load()
         h = ctypes.c_void_p()
         check(L.bri17_server_create(int(memory_budget_bytes), int(slots_per_bucket),
                                     ctypes.byref(h)), "bri17_server_create")
         self._h = h
+        if size_priority:
+            check(L.bri17_server_set_size_priority(h, 1), "bri17_server_set_size_priority")
         self._out = {}     # id -> solution array (kept alive until read)
         self._taus = {}
         self.pending = 0
