@@ -319,8 +319,8 @@ int bri17_server_destroy(bri17_server* srv);
  * Scheduling policy for buckets created from now on: 0 (default) all
  * streams equal, highest throughput; 1 smaller geometries on higher-priority
  * streams, so small requests are not queued behind large buckets' kernels
- * (on the 512-request benchmark stream: p50 latency 3.1 -> 0.9 s,
- * throughput 46 -> 42 solves/s).
+ * (on the 512-request benchmark stream: p50 latency 2.4 -> 0.5 s,
+ * throughput 51 -> 44 solves/s).
  */
 int bri17_server_set_size_priority(bri17_server* srv, int enable);
 
