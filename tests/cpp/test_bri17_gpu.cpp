@@ -126,7 +126,8 @@ int main(int argc, char** argv) {
     std::printf("exception: %s\n", e.what());
     return 1;
   }
-  // T = float instantiation of the header API: the FP32 operator
+  // T = float instantiation of the header API (`scaling` promoted to double,
+  // include/bri17/bri17.hpp:266): the FP32 operator
   // agrees with the FP64 one to FP32 accuracy, and the per-mode methods
   // return the FP64 values rounded to float.
   {
