@@ -187,9 +187,16 @@ class Hooke {
   void apply_stiffness(T const* u_dev, T* f_dev, cudaStream_t s = nullptr) const {
     detail::check(bri17_apply_stiffness(op_, u_dev, f_dev, s), "bri17_apply_stiffness");
   }
-  /** Same with host buffers (synchronous). */
+  /** Same with host buffers (synchronous; page-locked buffers are read and
+   *  written in place by the first and last passes). */
   void apply_stiffness_host(T const* u, T* f, cudaStream_t s = nullptr) const {
     detail::check(bri17_apply_stiffness_host(op_, u, f, s), "bri17_apply_stiffness_host");
+  }
+  /** T = double: apply_stiffness(_host) in float-pair arithmetic on the FP32
+   *  pipe (about 1e-14 from FP64); 3D power-of-two grids only. */
+  void set_float_pair(bool enable) {
+    static_assert(std::is_same<T, double>::value, "float pairs replace FP64 arithmetic");
+    detail::check(bri17_op_set_float_pair(op_, enable ? 1 : 0), "bri17_op_set_float_pair");
   }
   /** Cell strains (Mandel), compute_Bu (tests/test_bri17.cpp:194-245). */
   void apply_strain(T const* u_dev, T* eps_dev, cudaStream_t s = nullptr) const {
