@@ -322,7 +322,13 @@ class Hooke:
             raise TypeError("b must be an FP64 CUDA tensor")
         if b.numel() != d * self._grid.size or not b.is_contiguous():
             raise ValueError("b must be a contiguous (DIM, *shape) tensor")
-        x = torch.zeros_like(b) if x0 is None else x0.clone().contiguous()
+        if x0 is None:
+            x = torch.zeros_like(b)
+        else:
+            if (not torch.is_tensor(x0) or x0.device != b.device
+                    or x0.dtype != torch.float64 or x0.numel() != b.numel()):
+                raise ValueError("x0 must be an FP64 tensor on b's device with b's size")
+            x = x0.clone().reshape(b.shape).contiguous()
         info = _lib.CgInfo()
         rc = _lib.load().bri17_cg_solve(
             self._h, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr()),
