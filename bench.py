@@ -185,10 +185,11 @@ def fused_flops(shape, comps):
 # ---------------------------------------------------------------------------
 
 
-def cpu_reference_apply_time(workload, threads: int, reps: int):
+def cpu_reference_apply_time(workload, threads: int, reps: int, warmup: int = 1):
     """Time the oracle restatement of compute_Ku on the host: C2C FFTs
     (numpy pocketfft single-threaded, or scipy.fft with `threads` workers)
-    plus the per-mode loop in C with `threads` OpenMP threads."""
+    plus the per-mode loop in C with `threads` OpenMP threads.  `warmup`
+    untimed applications come first."""
     from oracle import oracle as O
     shape = workload["shape"]
     grid = O.Grid(shape, workload["L"])
@@ -218,7 +219,8 @@ def cpu_reference_apply_time(workload, threads: int, reps: int):
         ku *= grid.cell_volume / grid.size
         return ku.real
 
-    apply()
+    for _ in range(max(1, warmup)):
+        apply()
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -235,7 +237,7 @@ def run_reference(args):
     dof = 3 * int(np.prod(w["shape"]))
     threads = os.cpu_count() or 1
     # Warm-up then K timed steps; each step = one full application.
-    times = cpu_reference_apply_time(w, threads, max(1, args.steps))
+    times = cpu_reference_apply_time(w, threads, max(1, args.steps), args.warmup)
     total = sum(times)
     value = dof * len(times) / total / 1e9
     line = {
