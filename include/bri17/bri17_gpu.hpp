@@ -119,8 +119,9 @@ std::ostream& operator<<(std::ostream& os, const CartesianGrid<T, DIM>& g) {
  *  (include/bri17/bri17.hpp:176-356). */
 template <typename T, int DIM>
 class Hooke {
-  static_assert(std::is_floating_point<T>::value && (DIM == 2 || DIM == 3),
-                "Hooke<T, DIM>: T floating point, DIM 2 or 3");
+  static_assert((std::is_same<T, float>::value || std::is_same<T, double>::value) &&
+                    (DIM == 2 || DIM == 3),
+                "Hooke<T, DIM>: T float or double (the operator's field types), DIM 2 or 3");
 
  public:
   T const mu;
@@ -194,8 +195,9 @@ class Hooke {
   }
   /** T = double: apply_stiffness(_host) in float-pair arithmetic on the FP32
    *  pipe (about 1e-14 from FP64); 3D power-of-two grids only. */
+  template <typename U = T,
+            typename = typename std::enable_if<std::is_same<U, double>::value>::type>
   void set_float_pair(bool enable) {
-    static_assert(std::is_same<T, double>::value, "float pairs replace FP64 arithmetic");
     detail::check(bri17_op_set_float_pair(op_, enable ? 1 : 0), "bri17_op_set_float_pair");
   }
   /** Cell strains (Mandel), compute_Bu (tests/test_bri17.cpp:194-245). */

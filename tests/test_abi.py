@@ -77,3 +77,96 @@ def test_pybri17_surface_and_contiguity_checks():
         pybri17._check_contiguous(np.zeros((2, 2), np.complex128), np.complex128)
     with pytest.raises(ValueError):
         pybri17._check_contiguous(np.zeros(8, np.complex128)[::2], np.complex128)
+
+
+_CPP_USES = r"""
+#include <sstream>
+#include "bri17/bri17_gpu.hpp"
+
+template <typename T, int DIM>
+int exercise(bool run) {
+  if (!run) return 0;
+  std::array<int, DIM> n{};
+  std::array<T, DIM> L{};
+  n.fill(8);
+  L.fill(T(1));
+  bri17::CartesianGrid<T, DIM> g(n, L);
+  std::ostringstream os;
+  os << g;
+  int nodes = g.get_cell_nodes(0)[0];
+  if constexpr (DIM == 2) nodes += g.get_node_at(1, 2); else nodes += g.get_node_at(1, 2, 3);
+  bri17::Hooke<T, DIM> h(T(1), T(0.3), g);
+  bri17::Hooke<T, DIM> h2(h);
+  os << h << h2.repr();
+  constexpr int sym = bri17::Hooke<T, DIM>::sym;
+  int k[DIM] = {};
+  std::complex<T> B[DIM], K[DIM * DIM], tau[sym], eta[sym];
+  h.modal_strain_displacement(k, B);
+  h.modal_stiffness(k, K);
+  h.modal_eigenstress_to_opposite_strain(k, tau, eta);
+  T* p = nullptr;
+  h.apply_stiffness(p, p);
+  h.apply_stiffness_host(p, p);
+  h.apply_strain(p, p);
+  h.eigenstress_rhs(p, p);
+  h.eigenstress_to_opposite_strain(p, p);
+  double* d = nullptr;
+  bri17_cg_info info = h.cg_solve(d, d, 1e-8, 10, true);
+  if constexpr (std::is_same<T, double>::value) h.set_float_pair(false);
+  return nodes + info.iterations + (h.handle() != nullptr);
+}
+
+int main(int argc, char**) {
+  const bool run = argc > 1000;  // compiled and linked, never run here
+  return exercise<double, 2>(run) + exercise<double, 3>(run) + exercise<float, 2>(run) +
+         exercise<float, 3>(run);
+}
+"""
+
+
+def _nvcc():
+    import os
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc absent")
+    return nvcc
+
+
+def test_cpp_host_api_compiles_and_links(tmp_path):
+    """Every public member of include/bri17/bri17_gpu.hpp, for T = float and
+    double and DIM = 2 and 3, compiles and resolves against the library; so
+    does the GPU golden-test program (tests/cpp/test_bri17_gpu.cpp)."""
+    import os
+    import subprocess
+
+    from conftest import REPO
+    nvcc = _nvcc()
+    inc, lib_dir = os.path.join(REPO, "include"), os.path.join(REPO, "bri17_gb300")
+    link = ["-L", lib_dir, "-lbri17_gb300", f"-Xlinker=-rpath={lib_dir}"]
+    src = tmp_path / "uses.cpp"
+    src.write_text(_CPP_USES)
+    for s, exe in ((str(src), tmp_path / "uses"),
+                   (os.path.join(REPO, "tests", "cpp", "test_bri17_gpu.cpp"), tmp_path / "golden")):
+        r = subprocess.run([nvcc, "-std=c++17", "-O1", "-I", inc, s, "-o", str(exe), *link],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("body,why", [
+    ("bri17::Hooke<float, 3>* h = nullptr; h->set_float_pair(true);", "set_float_pair"),
+    ("bri17::Hooke<long double, 3>* h = nullptr; (void)h->mu;", "float or double"),
+])
+def test_cpp_host_api_rejects_unsupported_types(tmp_path, body, why):
+    """Float pairs exist only for FP64 handles, and the operator takes float
+    or double fields only: both misuses fail to compile."""
+    import os
+    import subprocess
+
+    from conftest import REPO
+    src = tmp_path / "bad.cpp"
+    src.write_text('#include "bri17/bri17_gpu.hpp"\nint main() { ' + body + " return 0; }\n")
+    r = subprocess.run([_nvcc(), "-std=c++17", "-I", os.path.join(REPO, "include"),
+                        "-c", str(src), "-o", str(tmp_path / "bad.o")],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and why in r.stderr, r.stderr
