@@ -42,8 +42,17 @@ def _headers_mtime() -> float:
     return max(os.path.getmtime(h) for h in hs)
 
 
+def _flags_tag(extra) -> str:
+    """Object-name suffix for extra nvcc flags, so that objects built with
+    other flags are never reused."""
+    if not extra:
+        return ""
+    import hashlib
+    return "." + hashlib.sha1("\0".join(extra).encode()).hexdigest()[:10]
+
+
 def _compile(src: str, extra) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    obj = os.path.join(BUILD, os.path.basename(src) + _flags_tag(extra) + ".o")
     if (os.path.exists(obj) and os.path.getmtime(obj) > os.path.getmtime(src)
             and os.path.getmtime(obj) > _headers_mtime()):
         return obj
@@ -61,7 +70,11 @@ def build(verbose: bool = False, extra=()) -> str:
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
-    if (not os.path.exists(LIB)
+    # The library records the objects it was linked from; another set (other
+    # sources or flags) relinks it.
+    stamp = os.path.join(BUILD, "libbri17_gb300.objs")
+    linked = open(stamp).read() if os.path.exists(stamp) else None
+    if (not os.path.exists(LIB) or linked != "\n".join(objs)
             or max(os.path.getmtime(o) for o in objs) > os.path.getmtime(LIB)):
         tmp = LIB + ".tmp"
         cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
@@ -69,6 +82,8 @@ def build(verbose: bool = False, extra=()) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+        with open(stamp, "w") as f:
+            f.write("\n".join(objs))
     if verbose:
         print("built", LIB)
     return LIB
