@@ -710,12 +710,13 @@ int submit_request(bri17_server* srv, const int* shape, const double* L, double 
     return BRI17_ERR_INVALID_ARGUMENT;
   }
   for (int i = 0; i < 3; i++)
-    if (shape[i] < 1 || shape[i] > 1024 || !(L[i] > 0)) {
-      set_error("shape entries must be in [1, 1024] and L entries positive");
+    if (shape[i] < 1 || shape[i] > 1024 || !(L[i] > 0) || !std::isfinite(L[i])) {
+      set_error("shape entries must be in [1, 1024] and L entries positive and finite");
       return BRI17_ERR_INVALID_ARGUMENT;
     }
-  if (!(mu > 0) || !(nu > -1.0 && nu < 0.5) || !(tol > 0) || max_iterations < 1) {
-    set_error("need mu > 0, -1 < nu < 0.5, tol > 0, max_iterations >= 1");
+  if (!(mu > 0) || !std::isfinite(mu) || !(nu > -1.0 && nu < 0.5) || !(tol > 0) ||
+      max_iterations < 1) {
+    set_error("need finite mu > 0, -1 < nu < 0.5, tol > 0, max_iterations >= 1");
     return BRI17_ERR_INVALID_ARGUMENT;
   }
   AxisPlan p;
@@ -958,6 +959,10 @@ extern "C" int bri17_server_poll(bri17_server* srv, bri17_request_result* out, i
                                  int* count) {
   if (!srv || (!out && cap > 0) || !count) {
     set_error("null pointer");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  if (cap < 0) {
+    set_error("cap must be >= 0");
     return BRI17_ERR_INVALID_ARGUMENT;
   }
   const int k = (int)std::min<size_t>(cap, srv->done.size());

@@ -354,7 +354,7 @@ int bri17_server_submit_borrowed(bri17_server* srv, const int* shape,
  * the number of active requests in *active. */
 int bri17_server_step(bri17_server* srv, int* active);
 
-/* Pop up to `cap` finished results; *count receives how many. */
+/* Pop up to `cap` (>= 0) finished results; *count receives how many. */
 int bri17_server_poll(bri17_server* srv, bri17_request_result* out, int cap,
                       int* count);
 

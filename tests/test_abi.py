@@ -170,3 +170,26 @@ def test_cpp_host_api_rejects_unsupported_types(tmp_path, body, why):
                         "-c", str(src), "-o", str(tmp_path / "bad.o")],
                        capture_output=True, text=True)
     assert r.returncode != 0 and why in r.stderr, r.stderr
+
+
+def test_server_argument_validation_before_device():
+    """bri17_server_* reject bad arguments and null handles before any
+    device call (the server's poll writes at most `cap` results)."""
+    L = _lib.load()
+    s = ctypes.c_void_p()
+    assert L.bri17_server_create(0, 8, ctypes.byref(s)) == 1
+    assert L.bri17_server_create(1 << 30, 0, ctypes.byref(s)) == 1
+    assert L.bri17_server_create(1 << 30, 257, ctypes.byref(s)) == 1
+    assert L.bri17_server_create(1 << 30, 8, None) == 1
+    n = ctypes.c_int()
+    rid = ctypes.c_int64()
+    shape = (ctypes.c_int * 3)(8, 8, 8)
+    Ls = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+    assert L.bri17_server_step(None, ctypes.byref(n)) == 1
+    assert L.bri17_server_poll(None, None, 0, ctypes.byref(n)) == 1
+    assert L.bri17_server_cancel(None, 0) == 1
+    assert L.bri17_server_set_size_priority(None, 1) == 1
+    assert L.bri17_server_submit(None, shape, Ls, 1.0, 0.3, None, None, 1e-8, 10,
+                                 ctypes.byref(rid)) == 1
+    assert L.bri17_server_destroy(None) == 0
+    assert L.bri17_server_clock(None) == 0.0

@@ -103,6 +103,16 @@ def test_submit_validation():
         srv.submit((8, 8, 8), (1, 1, 1), 1.0, 0.5, tau)      # nu = 0.5
     with pytest.raises(Bri17Error):
         srv.submit((256, 256, 256), (1, 1, 1), 1.0, 0.3, np.zeros(6 * 256 ** 3))
+    with pytest.raises(Bri17Error):
+        srv.submit((8, 8, 8), (1, float("inf"), 1), 1.0, 0.3, tau)  # non-finite L
+    with pytest.raises(Bri17Error):
+        srv.submit((8, 8, 8), (1, 1, 1), float("inf"), 0.3, tau)  # non-finite mu
+    import ctypes
+
+    from bri17_gb300 import _lib
+    n = ctypes.c_int()
+    assert _lib.load().bri17_server_poll(srv._h, (_lib.RequestResult * 1)(), -1,
+                                         ctypes.byref(n)) == 1   # negative cap
     rid = srv.submit((8, 8, 8), (1, 1, 1), 1.0, 0.3, tau)  # tau = 0 -> x = 0
     res = srv.run_until_idle()
     assert res[0]["status"] == 0 and np.all(srv.result(rid) == 0)
