@@ -76,6 +76,9 @@ def test_cg_warm_start_and_material_change():
     x, info = h.cg_solve(b, tol=1e-6)
     x2, info2 = h.cg_solve(b, x0=x, tol=1e-10)
     assert info2["iterations"] < 200 and info2["rel_residual"] <= 1e-10
+    for bad_x0 in (x.cpu(), x.float(), x[:2]):  # host memory, FP32, wrong size
+        with pytest.raises(ValueError):
+            h.cg_solve(b, x0=bad_x0)
     h.set_material(2.0, 0.2)
     ho2 = O.Hooke(2.0, 0.2, ho.grid)
     x3, info3 = h.cg_solve(b, tol=1e-10, mode="mixed")
