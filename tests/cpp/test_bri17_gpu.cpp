@@ -166,6 +166,38 @@ int main(int argc, char** argv) {
     passed += ok;
     total++;
   }
+  // Float-pair arithmetic on an FP64 handle (Hooke<double,3>::set_float_pair):
+  // within 1e-13 of the FP64 operator, and switching back gives the FP64
+  // result bit for bit.
+  {
+    bri17::CartesianGrid<double, 3> g{{64, 64, 128}, {1.0, 1.0, 2.0}};
+    bri17::Hooke<double, 3> h{1.0, 0.3, g};
+    const int n = 3 * g.size;
+    std::vector<double> u(n), f(n), fp(n), f2(n);
+    unsigned s = 777u;
+    for (int i = 0; i < n; i++) {
+      s = s * 1103515245u + 12345u;
+      u[i] = (double)((s >> 8) % 20001) / 10000.0 - 1.0;
+    }
+    h.apply_stiffness_host(u.data(), f.data());
+    h.set_float_pair(true);
+    h.apply_stiffness_host(u.data(), fp.data());
+    h.set_float_pair(false);
+    h.apply_stiffness_host(u.data(), f2.data());
+    double num = 0, den = 0;
+    bool same = true;
+    for (int i = 0; i < n; i++) {
+      num += (fp[i] - f[i]) * (fp[i] - f[i]);
+      den += f[i] * f[i];
+      same = same && f2[i] == f[i];
+    }
+    const double rel = std::sqrt(num / den);
+    const bool ok = rel <= 1e-13 && same;
+    std::printf("Hooke<double,3> float pairs: rel diff %.2e vs FP64, FP64 again %s: %s\n", rel,
+                same ? "identical" : "differs", ok ? "passed" : "FAILED");
+    passed += ok;
+    total++;
+  }
   std::printf("%d of %d sections passed\n", passed, total);
   return passed == total && total > 0 ? 0 : 1;
 }

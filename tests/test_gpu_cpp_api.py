@@ -34,4 +34,4 @@ def test_cpp_api_golden_sections(golden_elements, tmp_path):
     r = subprocess.run([str(exe), str(golden)], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "5 of 5 sections passed" in r.stdout
+    assert "6 of 6 sections passed" in r.stdout
