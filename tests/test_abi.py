@@ -77,6 +77,9 @@ def test_pybri17_surface_and_contiguity_checks():
         pybri17._check_contiguous(np.zeros((2, 2), np.complex128), np.complex128)
     with pytest.raises(ValueError):
         pybri17._check_contiguous(np.zeros(8, np.complex128)[::2], np.complex128)
+    with pytest.raises(TypeError):  # the reference would write into a temporary copy
+        pybri17._check_contiguous(np.zeros(4, np.complex64), np.complex128)
+    pybri17._check_contiguous(np.zeros(4, np.complex128), np.complex128)
 
 
 _CPP_USES = r"""
