@@ -33,11 +33,13 @@ __version__ = "0.1"
 
 def _check_contiguous(a, dtype):
     """python/pybri17.cpp:9-15: one-dimensional and contiguous, else
-    ValueError (std::invalid_argument maps to ValueError in pybind11)."""
+    ValueError (std::invalid_argument maps to ValueError in pybind11).  An
+    array of another dtype raises TypeError: the reference's py::array_t
+    would convert it to a temporary copy and write there."""
+    if isinstance(a, np.ndarray) and a.dtype != dtype:
+        raise TypeError(f"expected dtype {np.dtype(dtype)}, got {a.dtype}")
     if not isinstance(a, np.ndarray) or a.ndim != 1 or a.strides[0] != np.dtype(dtype).itemsize:
         raise ValueError("expected one-dimensional, contiguous array")
-    if a.dtype != dtype:
-        raise TypeError(f"expected dtype {np.dtype(dtype)}")
 
 
 class _GridBase(api.CartesianGrid):
