@@ -2,7 +2,7 @@
 
 Run in a container where the reference checkout is present:
 
-    python tests/golden/make_golden.py [--ref-root PATH]
+    python tests/golden/make_golden.py [--ref-root PATH] [--out-dir DIR]
 
 1. ``element_matrices.json``: the four Maxima element matrices that the
    reference's own test hard-codes (Ke 8x8 and 24x24, Be 3x8 and 6x24,
@@ -29,6 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
+DEFAULT_REF_ROOT = "/root/reference"
 sys.path.insert(0, REPO)
 
 
@@ -54,10 +55,13 @@ MODAL_CASES = [
 ]
 
 
-def main() -> None:
+def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
-    args = ap.parse_args()
+    ap.add_argument("--ref-root", default=DEFAULT_REF_ROOT)
+    ap.add_argument("--out-dir", default=HERE,
+                    help="where to write the fixtures (default: beside this script)")
+    args = ap.parse_args(argv)
+    out = args.out_dir
     test_src = os.path.join(args.ref_root, "tests", "test_bri17.cpp")
     with open(test_src) as f:
         src = f.read()
@@ -90,7 +94,7 @@ def main() -> None:
              "shape": shape3, "L": L3, "rows": 6, "cols": 24, "values": be[1]},
         ],
     }
-    with open(os.path.join(HERE, "element_matrices.json"), "w") as f:
+    with open(os.path.join(out, "element_matrices.json"), "w") as f:
         json.dump(golden, f, indent=1)
 
     subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "ref",
@@ -126,12 +130,12 @@ def main() -> None:
         arrays[f"B_{ci}"] = B
         arrays[f"nodes_{ci}"] = nodes
         meta.append(case)
-    np.savez_compressed(os.path.join(HERE, "modal_ref.npz"), **arrays)
-    with open(os.path.join(HERE, "modal_ref.json"), "w") as f:
+    np.savez_compressed(os.path.join(out, "modal_ref.npz"), **arrays)
+    with open(os.path.join(out, "modal_ref.json"), "w") as f:
         json.dump({"source": "include/bri17/bri17.hpp (sbrisard/bri17) compiled "
                              "unmodified by oracle/Makefile, -O2 -ffp-contract=off",
                    "cases": meta}, f, indent=1)
-    print("wrote", sorted(os.listdir(HERE)))
+    print("wrote", sorted(os.listdir(out)))
 
 
 if __name__ == "__main__":

@@ -194,3 +194,33 @@ def test_opposite_strain_field_restatement():
     assert np.abs(etahat[:, 0, 0, 0]).max() <= 1e-13 * np.abs(etahat).max()
     eps = O.apply_strain(h, O.eigenstress_solve(h, tau))
     assert np.abs(eta + eps).max() <= 1e-13 * np.abs(eta).max()
+
+
+def _make_golden():
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.mark.skipif(not __import__("os").path.isdir(_make_golden().DEFAULT_REF_ROOT),
+                    reason="needs the reference checkout")
+def test_golden_fixtures_regenerate_identically(tmp_path):
+    """tests/golden/make_golden.py, run again on the reference, writes the
+    committed fixtures: the same JSON text and bit-identical arrays."""
+    import os
+    mg = _make_golden()
+    mg.main(["--out-dir", str(tmp_path)])
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    for name in ("element_matrices.json", "modal_ref.json"):
+        with open(os.path.join(here, name)) as a, open(tmp_path / name) as b:
+            assert a.read() == b.read(), name
+    a = np.load(os.path.join(here, "modal_ref.npz"))
+    b = np.load(tmp_path / "modal_ref.npz")
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        assert a[k].dtype == b[k].dtype and np.array_equal(a[k].view(np.uint8),
+                                                           b[k].view(np.uint8)), k
