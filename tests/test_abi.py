@@ -196,3 +196,16 @@ def test_server_argument_validation_before_device():
                                  ctypes.byref(rid)) == 1
     assert L.bri17_server_destroy(None) == 0
     assert L.bri17_server_clock(None) == 0.0
+
+
+def test_integration_notes_cover_every_entry_point():
+    """INTEGRATION.md names every function the header declares (the server's
+    through its bri17_server_* row) with the interface it replaces."""
+    import os
+
+    from conftest import REPO
+    with open(os.path.join(REPO, "INTEGRATION.md")) as f:
+        doc = f.read()
+    missing = [s for s in _lib.declared_symbols() if s not in doc
+               and not (s.startswith("bri17_server_") and "bri17_server_*" in doc)]
+    assert not missing, missing
