@@ -68,11 +68,13 @@ typedef enum bri17_precision {
 
 typedef struct bri17_op bri17_op; /* opaque operator handle */
 
-/* Human-readable name of a status code (static storage). */
+/* Human-readable name of a status code (static storage).  No reference
+ * counterpart: the reference returns no status and throws only from
+ * unreachable branches (include/bri17/bri17.hpp:154-156). */
 const char* bri17_status_string(int status);
 
 /* Last CUDA / validation message recorded by this thread (static storage per
- * thread; empty string if none). */
+ * thread; empty string if none).  No reference counterpart. */
 const char* bri17_last_error(void);
 
 /* Library version string, e.g. "0.1.0" (the reference is v0.1,
@@ -93,10 +95,13 @@ const char* bri17_version(void);
 int bri17_op_create(int dim, const int* shape, const double* L, double mu,
                     double nu, int precision, bri17_op** op);
 
-/* Release a handle and its device memory (NULL is accepted). */
+/* Release a handle and its device memory (NULL is accepted).  Replaces the
+ * end of life of the bri17::Hooke value and of the FFT buffers
+ * (~FFTWComplexBuffer, tests/test_bri17.cpp:40). */
 int bri17_op_destroy(bri17_op* op);
 
-/* Grid size |N| (number of nodes = cells) and device work-space bytes. */
+/* Grid size |N| (number of nodes = cells; CartesianGrid::size,
+ * include/bri17/bri17.hpp:54-58) and device work-space bytes. */
 int bri17_op_info(const bri17_op* op, int64_t* size, int64_t* workspace_bytes);
 
 /*
@@ -113,7 +118,9 @@ int bri17_op_pass_times(bri17_op* op, double* ms, int64_t* launches,
                         int max_passes, int* npasses);
 const char* bri17_pass_name(int pass);
 
-/* Change the material of an existing handle (no reallocation). */
+/* Change the material of an existing handle (no reallocation).  Replaces
+ * constructing a new bri17::Hooke(mu, nu, grid) on the same grid
+ * (include/bri17/bri17.hpp:193-194); same bounds as bri17_op_create. */
 int bri17_op_set_material(bri17_op* op, double mu, double nu);
 
 /*
@@ -148,6 +155,7 @@ int bri17_op_set_float_pair(bri17_op* op, int enable);
  * Bounded device-side waits (tensor-copy completions) that ran out on the
  * current device since the previous call; 0 in normal operation.  A nonzero
  * count means some operator results of that period are invalid.
+ * Diagnostics; no reference counterpart.
  */
 int bri17_wait_timeouts(int* count);
 
@@ -218,7 +226,8 @@ int bri17_apply_stiffness_noalloc(int dim, const int* shape, const double* L,
 
 /*
  * Same operator with host buffers; synchronises `stream` before returning.
- * Page-locked buffers (cudaHostAlloc / cudaHostRegister) are read and written
+ * Replaces compute_Ku called on host data (tests/test_bri17.cpp:56-107), the
+ * form a binding that owns numpy arrays would call.  Page-locked buffers (cudaHostAlloc / cudaHostRegister) are read and written
  * in place by the first and last passes over the host link; other host
  * memory goes through device staging buffers with the copies pipelined per
  * component against the passes.
@@ -275,6 +284,10 @@ typedef struct bri17_cg_info {
 } bri17_cg_info;
 
 /*
+ * No reference counterpart as an iterative solver: the reference solves the
+ * eigenstress problem mode by mode (python/demo.py:24-40 over
+ * Hooke::modal_eigenstress_to_opposite_strain, include/bri17/bri17.hpp:308-355),
+ * which is this library's oracle for it.
  * Solve K x = b by conjugate gradients, to ||b - K x|| <= tol ||b||, with x
  * projected to zero mean per component (the null space of K is the rigid
  * translations, sphinx/theory.rst eq. (17) note).  b_dev and x_dev are FP64
@@ -288,7 +301,8 @@ int bri17_cg_solve(bri17_op* op, const double* b_dev, double* x_dev,
                    bri17_cg_info* info, void* stream);
 
 /*
- * Serving: a continuous-batching solve server on the current device.
+ * Serving (no reference counterpart): a continuous-batching solve server on
+ * the current device.
  * Requests (3D eigenstress problems of any supported grid and material) are
  * admitted while their device footprint fits in `memory_budget_bytes`,
  * solved concurrently in mixed precision, and retired when converged.
