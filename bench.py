@@ -233,8 +233,17 @@ def run_reference(args):
     ws, rank, local = dist_env()
     if ws > 1 and rank != 0:
         return 0
-    w = WORKLOAD_128
-    dof = 3 * int(np.prod(w["shape"]))
+    if args.workload not in ("operator", "operator_f32"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"--workload {args.workload}: the reference has no CG solver or "
+                          "request server (its eigenstress solve is the per-mode direct "
+                          "one); its CPU operator path is timed by --workload operator"}))
+        return 0
+    w = dict(WORKLOAD_128)
+    if args.shape:
+        w["shape"] = tuple(int(n) for n in args.shape.split("x"))
+        w["L"] = (1.0,) * len(w["shape"])
+    dof = len(w["shape"]) * int(np.prod(w["shape"]))
     threads = os.cpu_count() or 1
     # Warm-up then K timed steps; each step = one full application.
     times = cpu_reference_apply_time(w, threads, max(1, args.steps), args.warmup)
@@ -247,8 +256,9 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_of(w, args.gpus),
         "cpu_baseline": {"value": value, "unit": "GDoF/s", "cores": threads, "kind": "port",
-                         "sample": f"{len(times)} full 128^3 FP64 applications "
-                                   "(C2C scipy.fft + OpenMP per-mode loop)"},
+                         "sample": f"{len(times)} full {'x'.join(map(str, w['shape']))} FP64 "
+                                   "applications (C2C scipy.fft + OpenMP per-mode loop; "
+                                   "the reference computes in FP64 only)"},
         "e2e": {"value": value, "unit": "GDoF/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }

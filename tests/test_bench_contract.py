@@ -45,3 +45,19 @@ def test_reference_arm_other_ranks_exit_without_work():
              "--gpus", "2", "--steps", "1", "--warmup", "3")
     assert p.returncode == 0, p.stderr
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_follows_shape_and_names_unavailable_workloads():
+    for shape in ("32x32x32", "64x64"):
+        p = _run({}, "--shape", shape, "--steps", "1", "--warmup", "3")
+        assert p.returncode == 0, p.stderr
+        d = json.loads(p.stdout.strip().splitlines()[-1])
+        dims = [int(n) for n in shape.split("x")]
+        assert d["config"]["grid"] == dims
+        assert d["config"]["dof_per_step"] == len(dims) * int(__import__("math").prod(dims))
+        assert shape in d["cpu_baseline"]["sample"]
+    for workload in ("cg", "aniso", "serve"):
+        p = _run({}, "--workload", workload, "--steps", "1", "--warmup", "3")
+        assert p.returncode == 0, p.stderr
+        d = json.loads(p.stdout.strip())
+        assert d["impl"] == "reference" and "unavailable" in d and workload in d["unavailable"]
