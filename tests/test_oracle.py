@@ -224,3 +224,22 @@ def test_golden_fixtures_regenerate_identically(tmp_path):
     for k in a.files:
         assert a[k].dtype == b[k].dtype and np.array_equal(a[k].view(np.uint8),
                                                            b[k].view(np.uint8)), k
+
+
+def test_oracle_results_do_not_depend_on_thread_count():
+    """The per-mode loops split modes across OpenMP threads; every mode is
+    independent, so the operator's output is bit-identical for 1 and 4
+    threads (the CPU baselines time both)."""
+    rng = np.random.default_rng(21)
+    grid = O.Grid((12, 10, 9), (1.0, 0.8, 1.1))
+    h = O.Hooke(1.0, 0.3, grid)
+    u = rng.standard_normal((3,) + grid.shape)
+    before = O.num_threads()
+    try:
+        O.set_num_threads(1)
+        f1 = O.apply_stiffness(h, u)
+        O.set_num_threads(4)
+        f4 = O.apply_stiffness(h, u)
+    finally:
+        O.set_num_threads(before)
+    assert np.array_equal(f1.view(np.uint8), f4.view(np.uint8))
