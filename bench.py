@@ -449,7 +449,8 @@ def run_operator(args, precision="f64"):
     if dom:
         avg_ms = passes[dom]["ms_total"] / passes[dom]["launches"]
         ach = pb[dom] / (avg_ms * 1e-3) / 1e9
-        wl = f"{precision}_128cubed"
+        # Captured traffic exists for the 128^3 workload only (null otherwise).
+        wl = f"{precision}_128cubed" if tuple(shape) == (128, 128, 128) else None
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm_peak,
                 "traffic": traffic_from_profiles(dom, wl),
