@@ -243,3 +243,30 @@ def test_oracle_results_do_not_depend_on_thread_count():
     finally:
         O.set_num_threads(before)
     assert np.array_equal(f1.view(np.uint8), f4.view(np.uint8))
+
+
+DEGENERATE = [(0, (2, 2)), (0, (1, 5)), (0, (2, 3)), (0, (1, 1)),
+              (1, (2, 2, 2)), (1, (1, 3, 2)), (1, (2, 1, 4)), (1, (1, 1, 3)),
+              (2, (2, 2)), (2, (1, 5)), (3, (2, 2, 2)), (3, (1, 3, 2))]
+
+
+@pytest.mark.parametrize("case_index,shape", DEGENERATE)
+def test_golden_element_matrices_on_degenerate_grids(golden_elements, case_index, shape):
+    """The Maxima element matrices depend only on the cell spacing, so the
+    reference's golden check (tests/test_bri17.cpp:318-606) extends to other
+    grids of the same spacing: axes of one and two cells, where a cell's
+    periodic vertices coincide (include/bri17/bri17.hpp:127-158), at the
+    reference's tolerance."""
+    g = golden_elements
+    case = g["cases"][case_index]
+    spacing = [L / n for L, n in zip(case["L"], case["shape"])]
+    grid = O.Grid(shape, [n * s for n, s in zip(shape, spacing)])
+    hooke = O.Hooke(g["mu"], g["nu"], grid)
+    E = np.array(case["values"]).reshape(case["rows"], case["cols"])
+    if case["kind"] == "K":
+        expected = O.assemble_stiffness(grid, E)
+        actual = O.stiffness_matrix(hooke, imag_tol=g["imag_tol"])
+    else:
+        expected = O.assemble_strain_displacement(grid, E)
+        actual = O.strain_displacement_matrix(hooke, imag_tol=g["imag_tol"])
+    _assert_close(expected, actual, g["rtol"], g["atol"])
