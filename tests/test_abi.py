@@ -209,3 +209,27 @@ def test_integration_notes_cover_every_entry_point():
     missing = [s for s in _lib.declared_symbols() if s not in doc
                and not (s.startswith("bri17_server_") and "bri17_server_*" in doc)]
     assert not missing, missing
+
+
+def test_product_never_uses_the_oracle():
+    """The package and the library never import, link or load the CPU oracle
+    (no CPU fallback): no Python module of bri17_gb300 imports `oracle`, and
+    the shared library's dynamic dependencies name no oracle library."""
+    import ast
+    import os
+    import subprocess
+
+    from conftest import REPO
+    pkg = os.path.join(REPO, "bri17_gb300")
+    for name in os.listdir(pkg):
+        if not name.endswith(".py"):
+            continue
+        tree = ast.parse(open(os.path.join(pkg, name)).read())
+        for node in ast.walk(tree):
+            if isinstance(node, ast.Import):
+                assert not any(a.name.split(".")[0] == "oracle" for a in node.names), name
+            elif isinstance(node, ast.ImportFrom):
+                assert (node.module or "").split(".")[0] != "oracle", name
+    r = subprocess.run(["ldd", _lib.LIB_PATH], capture_output=True, text=True)
+    if r.returncode == 0:
+        assert "oracle" not in r.stdout and "bri17_ref" not in r.stdout
