@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
 #include <string>
 
 #include "../../include/bri17_gb300.h"
@@ -66,5 +68,30 @@ inline void set_p8_plans(Geometry* g) {
 }
 
 bool make_plan(int n, AxisPlan* p);
+
+// Runs f() once for each CUDA device it is called with current.  Kernel
+// attributes (the dynamic shared-memory limit among them) belong to a
+// device, so they are set again on every device a process uses.  `done`
+// holds one bit per device ordinal below 64; higher ordinals run f() on
+// every call.
+template <typename F>
+void once_per_device(std::atomic<unsigned long long>* done, F&& f) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (dev < 0 || dev >= 64) {
+    f();
+    return;
+  }
+  const unsigned long long bit = 1ull << dev;
+  if (done->load(std::memory_order_acquire) & bit) return;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done->load(std::memory_order_relaxed) & bit) return;
+  f();
+  done->fetch_or(bit, std::memory_order_release);
+}
 
 }  // namespace bri17gb

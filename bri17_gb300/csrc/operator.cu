@@ -195,8 +195,8 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 template <typename T>
 static void set_smem_attrs() {
-  static std::once_flag once;
-  std::call_once(once, [] {
+  static std::atomic<unsigned long long> done{0};
+  once_per_device(&done, [] {
     cudaFuncSetAttribute(rows_r2c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(rows_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(axis_c2c<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
@@ -1371,8 +1371,8 @@ extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
       return cuda_fail(e, "cudaMemcpy(float-pair tables)");
     }
     op->table_df = mem;
-    static std::once_flag once;
-    std::call_once(once, [] {
+    static std::atomic<unsigned long long> done{0};
+    once_per_device(&done, [] {
       ct_set_smem_attrs_df_rows(kMaxSmem);
       ct_set_smem_attrs_df_c2c(kMaxSmem);
       ct_set_smem_attrs_df_axis0(kMaxSmem);

@@ -427,6 +427,41 @@ void oracle_eigenstress_modal_solve(int dim, const int* shape, const double* L,
   }
 }
 
+/* The same modal direct solve over the half spectrum of a real field: the
+ * last axis holds only k_last in [0, shape[dim-1]/2] (the layout of a
+ * real-to-complex DFT), every other axis its full range.  tauhat is
+ * sym x (size / shape[dim-1] * H) complex (SoA) with H = shape[dim-1]/2 + 1,
+ * uhat DIM x that.  Every mode k is solved exactly as by
+ * oracle_eigenstress_modal_solve; the modes left out are the complex
+ * conjugates of kept ones (K(-k) = K(k), B(-k) = conj(B(k))), which the
+ * inverse real DFT restores. */
+void oracle_eigenstress_modal_solve_half(int dim, const int* shape, const double* L,
+                                         double mu, double nu, const double* tauhat,
+                                         double* uhat) {
+  oracle_hooke h;
+  make_hooke(&h, dim, shape, L, mu, nu);
+  oracle_hooke hh = h;
+  hh.shape[dim - 1] = shape[dim - 1] / 2 + 1;
+  int64_t size = 1;
+  for (int i = 0; i < dim; i++) size *= hh.shape[i];
+  const int sym = dim == 2 ? 3 : 6;
+#pragma omp parallel for schedule(static)
+  for (int64_t m = 0; m < size; m++) {
+    int k[3];
+    double tau[12], u[6], eta[12];
+    unflatten(&hh, m, k);
+    for (int s = 0; s < sym; s++) {
+      tau[2 * s] = tauhat[2 * (s * size + m)];
+      tau[2 * s + 1] = tauhat[2 * (s * size + m) + 1];
+    }
+    eigenstress_solve(&h, k, tau, u, eta);
+    for (int j = 0; j < dim; j++) {
+      uhat[2 * (j * size + m)] = u[2 * j];
+      uhat[2 * (j * size + m) + 1] = u[2 * j + 1];
+    }
+  }
+}
+
 /* Opposite strain in Fourier space over the full spectrum: eta_hat[k] =
  * Hooke::modal_eigenstress_to_opposite_strain(k, tau_hat[k])
  * (include/bri17/bri17.hpp:308-355), the per-mode loop of

@@ -45,14 +45,19 @@ _ip = ctypes.POINTER(ctypes.c_int)
 
 
 def build(quiet: bool = True) -> None:
-    """Compile the C restatement (and, where the reference is present, the
-    reference header) with ``make -C oracle``."""
+    """Compile the C restatement (and, where the reference checkout is
+    present, the reference header) with ``make -C oracle``."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", _HERE, "all"], check=True, stdout=out)
-    ref_root = os.environ.get("BRI17_REF_ROOT", "/root/reference")
-    if os.path.isfile(os.path.join(ref_root, "include", "bri17", "bri17.hpp")):
-        subprocess.run(["make", "-C", _HERE, "ref", f"REF_ROOT={ref_root}"],
-                       check=True, stdout=out)
+    subprocess.run(["make", "-C", _HERE, "ref-if-present"], check=True, stdout=out)
+
+
+def ref_root() -> str:
+    """Where oracle/Makefile reads the reference checkout (BRI17_REF_ROOT
+    overrides its default)."""
+    r = subprocess.run(["make", "-s", "-C", _HERE, "print-ref-root"],
+                       capture_output=True, text=True, check=True)
+    return r.stdout.strip()
 
 
 def lib() -> ctypes.CDLL:
@@ -71,7 +76,7 @@ def lib() -> ctypes.CDLL:
                 getattr(L, name).argtypes = common + [_ip, ctypes.c_int64, _dp]
             for name in ("oracle_stiffness_modal_apply", "oracle_strain_modal_apply",
                          "oracle_eigenstress_modal_solve", "oracle_eigenstress_modal_rhs",
-                         "oracle_eigenstress_modal_eta"):
+                         "oracle_eigenstress_modal_eta", "oracle_eigenstress_modal_solve_half"):
                 getattr(L, name).argtypes = common + [_dp, _dp]
             L.oracle_get_cell_nodes.argtypes = [ctypes.c_int, _ip, ctypes.c_int, _ip]
             L.oracle_get_node_at.argtypes = [ctypes.c_int, _ip, _ip]
@@ -311,6 +316,42 @@ def eigenstress_solve(hooke: Hooke, tau):
     tauhat = np.fft.fftn(tau.astype(np.complex128), axes=_axes(g.dim))
     uhat = hooke._modal_loop(lib().oracle_eigenstress_modal_solve, tauhat, g.dim)
     return -np.fft.ifftn(uhat, axes=_axes(g.dim)).real
+
+
+def eigenstress_solve_half(hooke: Hooke, tau, workers: int = 1):
+    """The solution of ``eigenstress_solve`` through real-to-complex DFTs:
+    only the half spectrum k_last in [0, N_last/2] is transformed and solved
+    (oracle_eigenstress_modal_solve_half, every kept mode as in
+    include/bri17/bri17.hpp:308-341), and the inverse real DFT restores the
+    conjugate half.  Same result to rounding, with half the transform work
+    and ``workers`` FFT threads (scipy.fft where present), so that it runs at
+    the large grids of the solver measurements."""
+    g = hooke.grid
+    tau = np.asarray(tau, dtype=np.float64).reshape((-1,) + g.shape)
+    axes = _axes(g.dim)
+    try:
+        import scipy.fft as sf
+
+        def rfftn(a):
+            return sf.rfftn(a, axes=axes, workers=workers)
+
+        def irfftn(a):
+            return sf.irfftn(a, s=g.shape, axes=axes, workers=workers)
+    except ImportError:  # numpy's pocketfft, one thread
+        def rfftn(a):
+            return np.fft.rfftn(a, axes=axes)
+
+        def irfftn(a):
+            return np.fft.irfftn(a, s=g.shape, axes=axes)
+    tauhat = np.ascontiguousarray(rfftn(tau), dtype=np.complex128)
+    del tau
+    hshape = g.shape[:-1] + (g.shape[-1] // 2 + 1,)
+    uhat = np.empty((g.dim,) + hshape, dtype=np.complex128)
+    args, keep = hooke._common()
+    lib().oracle_eigenstress_modal_solve_half(*args, tauhat.ctypes.data_as(_dp),
+                                              uhat.ctypes.data_as(_dp))
+    del tauhat
+    return -irfftn(uhat)
 
 
 def eigenstress_opposite_strain(hooke: Hooke, tau):

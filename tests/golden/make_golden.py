@@ -29,8 +29,14 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-DEFAULT_REF_ROOT = "/root/reference"
 sys.path.insert(0, REPO)
+
+
+def default_ref_root() -> str:
+    """The reference checkout this script reads: where oracle/Makefile
+    reads it (BRI17_REF_ROOT overrides)."""
+    from oracle import oracle as O
+    return O.ref_root()
 
 
 def parse_blocks(src: str, name: str):
@@ -57,10 +63,12 @@ MODAL_CASES = [
 
 def main(argv=None) -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default=DEFAULT_REF_ROOT)
+    ap.add_argument("--ref-root", default=None)
     ap.add_argument("--out-dir", default=HERE,
                     help="where to write the fixtures (default: beside this script)")
     args = ap.parse_args(argv)
+    if args.ref_root is None:
+        args.ref_root = default_ref_root()
     out = args.out_dir
     test_src = os.path.join(args.ref_root, "tests", "test_bri17.cpp")
     with open(test_src) as f:

@@ -198,16 +198,25 @@ def test_server_argument_validation_before_device():
     assert L.bri17_server_clock(None) == 0.0
 
 
-def test_integration_notes_cover_every_entry_point():
-    """INTEGRATION.md names every function the header declares (the server's
-    through its bri17_server_* row) with the interface it replaces."""
-    import os
-
-    from conftest import REPO
-    with open(os.path.join(REPO, "INTEGRATION.md")) as f:
-        doc = f.read()
-    missing = [s for s in _lib.declared_symbols() if s not in doc
-               and not (s.startswith("bri17_server_") and "bri17_server_*" in doc)]
+def test_header_cites_the_reference_for_every_entry_point():
+    """Every function the public header declares comes after a comment that
+    either cites the reference interface it replaces (a file:line of the
+    reference) or says that it has no reference counterpart.  A group of
+    declarations shares the comment above the group."""
+    import re
+    with open(_lib.HEADER) as f:
+        src = f.read()
+    cite = re.compile(r"(bri17\.hpp|test_bri17\.cpp|pybri17\.cpp|demo\.py|version\.txt)"
+                      r":\d+|:\d+-\d+|[Nn]o (reference )?counterpart|no counterpart")
+    missing = []
+    for name in _lib.declared_symbols():
+        m = re.search(r"\b" + name + r"\s*\(", re.sub(r"/\*.*?\*/", lambda c: " " * len(
+            c.group(0)), src, flags=re.S))
+        assert m, name
+        comments = list(re.finditer(r"/\*.*?\*/", src[:m.start()], flags=re.S))
+        text = re.sub(r"\s*\n\s*\*?\s*", " ", comments[-1].group(0)) if comments else ""
+        if not cite.search(text):
+            missing.append(name)
     assert not missing, missing
 
 
