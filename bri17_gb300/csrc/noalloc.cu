@@ -9,7 +9,9 @@
 // bri17_apply_stiffness_noalloc serves them: it takes the same inputs and
 // outputs, allocates nothing, and keeps its scratch (per-axis tables + the
 // half spectrum) in the fixed-size device array below, which every GPU that
-// loads this library holds until the process exits.
+// loads this library holds until the process exits.  A small kernel writes
+// the tables into that array on the caller's stream, so a call makes no
+// host-to-device copy and returns without waiting for the GPU.
 #include <math.h>
 #include <string.h>
 
@@ -32,11 +34,7 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 constexpr int kMaxDevices = 64;
 void* g_scratch_addr[kMaxDevices];
 
-// Host staging of the tables (3 axes x 1024 points x 72 bytes + padding).
-constexpr size_t kTableStageBytes = 256 * 1024;
-alignas(16) unsigned char g_table_stage[kTableStageBytes];
-
-std::mutex g_mu;  // guards g_scratch_addr and g_table_stage
+std::mutex g_mu;  // guards g_scratch_addr
 
 constexpr double kPiNA = 3.141592653589793238462643383279502884;
 
@@ -91,45 +89,61 @@ size_t table_bytes(const int* n, int dim) {
   return b;
 }
 
-// FP64 tables into `host`, with device pointers into `dev`: the same values
-// and layout as the allocating operator's tables.
-void fill_tables_fixed(const int* n, const double* L, int dim, unsigned char* host,
-                       unsigned char* dev, Tables<double>* tab) {
-  const long double pil = 3.141592653589793238462643383279502884L;
+// Device pointers of the FP64 tables inside the scratch array at `dev`, in
+// the allocating operator's layout: per axis the twiddles, the half-angle
+// unit vectors, then phi, chi, psi, cos(alpha), sin(alpha) N / L.
+void table_layout(const int* n, int dim, unsigned char* dev, Tables<double>* tab) {
   memset(tab, 0, sizeof(*tab));
   size_t off = 0;
   for (int i = 0; i < dim; i++) {
     const int m = n[i];
-    const double h = L[i] / m;
-    double2* tw = reinterpret_cast<double2*>(host + off);
     tab->tw[i] = reinterpret_cast<const double2*>(dev + off);
     off = a16(off + m * sizeof(double2));
-    double2* ea = reinterpret_cast<double2*>(host + off);
     tab->ea[i] = reinterpret_cast<const double2*>(dev + off);
     off = a16(off + m * sizeof(double2));
-    double* t5[5];
     const double** d5[5] = {&tab->kphi[i], &tab->kchi[i], &tab->kpsi[i], &tab->bc[i],
                             &tab->bs[i]};
     for (int j = 0; j < 5; j++) {
-      t5[j] = reinterpret_cast<double*>(host + off);
       *d5[j] = reinterpret_cast<const double*>(dev + off);
       off = a16(off + m * sizeof(double));
     }
-    for (int k = 0; k < m; k++) {
-      const long double ang = 2.0L * pil * (long double)k / (long double)m;
-      tw[k].x = (double)cosl(ang);
-      tw[k].y = (double)-sinl(ang);
-      const double beta = 2 * kPiNA * k / m;
-      t5[0][k] = 2 * (1 - cos(beta)) / h / h;
-      t5[1][k] = (2 + cos(beta)) / 3;
-      t5[2][k] = sin(beta) / h;
-      const double alpha = kPiNA * k / m;
-      t5[3][k] = cos(alpha);
-      t5[4][k] = sin(alpha) * m / L[i];
-      ea[k].x = cos(alpha);
-      ea[k].y = sin(alpha);
-    }
   }
+}
+
+struct TableArgs {
+  Tables<double> tab;
+  int dim;
+  int n[3];
+  double L[3];
+};
+
+// Writes the tables on the device, one thread per (axis, k), so that the
+// call needs no host buffer and no host-to-device copy.  The values are
+// those of the allocating operator's tables to within rounding: phi, chi,
+// psi and the half-angle factors follow Hooke::modal_stiffness and
+// Hooke::modal_strain_displacement (include/bri17/bri17.hpp:217-224,
+// :258-264); the twiddles exp(-2 pi i k / n) come from sincospi, whose
+// argument 2k/n carries the only rounding.
+__global__ void noalloc_fill_tables(TableArgs a) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = 0;
+  while (i < a.dim && t >= a.n[i]) t -= a.n[i++];
+  if (i >= a.dim) return;
+  const int m = a.n[i], k = t;
+  const double h = a.L[i] / m;
+  double s, c;
+  sincospi(2.0 * k / m, &s, &c);
+  const_cast<double2*>(a.tab.tw[i])[k] = make_double2(c, -s);
+  const double beta = 2 * kPiNA * k / m;
+  const double cb = cos(beta);
+  const_cast<double*>(a.tab.kphi[i])[k] = 2 * (1 - cb) / h / h;
+  const_cast<double*>(a.tab.kchi[i])[k] = (2 + cb) / 3;
+  const_cast<double*>(a.tab.kpsi[i])[k] = sin(beta) / h;
+  const double alpha = kPiNA * k / m;
+  const double ca = cos(alpha), sa = sin(alpha);
+  const_cast<double*>(a.tab.bc[i])[k] = ca;
+  const_cast<double*>(a.tab.bs[i])[k] = sa * m / a.L[i];
+  const_cast<double2*>(a.tab.ea[i])[k] = make_double2(ca, sa);
 }
 
 int fail(int status, const char* msg) {
@@ -175,7 +189,7 @@ extern "C" int bri17_apply_stiffness_noalloc(int dim, const int* shape, const do
   const size_t tbytes = table_bytes(g.n, dim);
   const size_t spec_off = (tbytes + 255) & ~size_t(255);
   const size_t need = spec_off + (size_t)dim * g.cspec * sizeof(double2);
-  if (need > kNoAllocScratchBytes || tbytes > kTableStageBytes)
+  if (need > kNoAllocScratchBytes)
     return fail(BRI17_ERR_UNSUPPORTED_SIZE,
                 "grid too large for the no-alloc entry point: it needs more than its fixed "
                 "64 MiB device scratch (tables + FP64 half spectrum); use bri17_apply_stiffness");
@@ -191,21 +205,32 @@ extern "C" int bri17_apply_stiffness_noalloc(int dim, const int* shape, const do
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return fail(BRI17_ERR_CUDA, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
-    // Once per device, with that device current: the device address of the
-    // scratch array.
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    g_scratch_addr[dev] = p;
+  unsigned char* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_scratch_addr[dev]) {
+      // Once per device, with that device current: the device address of the
+      // scratch array.
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+      g_scratch_addr[dev] = p;
+    }
+    scratch = static_cast<unsigned char*>(g_scratch_addr[dev]);
   }
-  unsigned char* scratch = static_cast<unsigned char*>(g_scratch_addr[dev]);
-  fill_tables_fixed(g.n, view.L, dim, g_table_stage, scratch, &view.tab64);
+  TableArgs ta;
+  table_layout(g.n, dim, scratch, &ta.tab);
+  view.tab64 = ta.tab;
+  ta.dim = dim;
+  int total = 0;
+  for (int i = 0; i < 3; i++) {
+    ta.n[i] = g.n[i];
+    ta.L[i] = view.L[i];
+    if (i < dim) total += g.n[i];
+  }
   cudaStream_t st = (cudaStream_t)stream;
-  // Pageable source: the call returns once the staging buffer is consumed,
-  // so g_table_stage may be refilled by the next call.
-  e = cudaMemcpyAsync(scratch, g_table_stage, tbytes, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(tables)");
+  noalloc_fill_tables<<<(total + 127) / 128, 128, 0, st>>>(ta);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "noalloc_fill_tables launch");
   return apply_stiffness_batched_async(&view, 1, u_dev, f_dev, scratch + spec_off, nullptr, st);
 }

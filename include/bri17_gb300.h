@@ -208,17 +208,19 @@ int bri17_apply_stiffness(bri17_op* op, const void* u_dev, void* f_dev,
  * caller that must not let cudaMalloc/cudaFree synchronise the device.
  * The caller passes the grid, the material, u_dev and f_dev (dim x size FP64
  * device arrays, SoA, as bri17_apply_stiffness); results equal
- * bri17_apply_stiffness's.
+ * bri17_apply_stiffness's to rounding (within 1e-12 relative).
  * Scratch (per-axis tables + the FP64 half spectrum) lives in one fixed
  * 64 MiB device array that every GPU loading this library holds until the
  * process exits; grids needing more (tables + dim * n0 * n1 * (n2/2+1) * 16
  * bytes, e.g. anything above 128^3) return BRI17_ERR_UNSUPPORTED_SIZE.
- * The first call on a device looks up that array's device address on that
- * device (set-up), so make the first call before any stream capture.  Every
- * call shares the one array and rewrites all of it that it reads (nothing
- * needs to start at zero); calls whose GPU work overlaps -- on different
- * streams, or from different threads -- race on it and must be serialised by
- * the caller.
+ * The tables are written into that array by a kernel on `stream`, so the
+ * call copies nothing from the host and is stream-ordered like
+ * bri17_apply_stiffness.  The first call on a device looks up that array's
+ * device address on that device (set-up), so make the first call before
+ * any stream capture.  Every call shares the one array and rewrites all of
+ * it that it reads (nothing needs to start at zero); calls whose GPU work
+ * overlaps -- on different streams, or from different threads -- race on it
+ * and must be serialised by the caller.
  */
 int bri17_apply_stiffness_noalloc(int dim, const int* shape, const double* L,
                                   double mu, double nu, const double* u_dev,
@@ -321,6 +323,7 @@ typedef struct bri17_request_result {
 } bri17_request_result;
 
 /*
+ * Create / destroy a server (no reference counterpart).
  * max_active (1..256): most request slots per bucket (one bucket per grid
  * geometry).  A bucket gets enough slots for about 48 M unknowns of batched
  * work per iteration, at least 8, at most max_active.
@@ -330,7 +333,7 @@ int bri17_server_create(int64_t memory_budget_bytes, int max_active,
 int bri17_server_destroy(bri17_server* srv);
 
 /*
- * Scheduling policy for buckets created from now on: 0 (default) all
+ * Scheduling policy (no reference counterpart) for buckets created from now on: 0 (default) all
  * streams equal, highest throughput; 1 smaller geometries on higher-priority
  * streams, so small requests are not queued behind large buckets' kernels
  * (on the 512-request benchmark stream: p50 latency 2.4 -> 0.5 s,
@@ -339,7 +342,8 @@ int bri17_server_destroy(bri17_server* srv);
 int bri17_server_set_size_priority(bri17_server* srv, int enable);
 
 /*
- * Submit one eigenstress solve.  tau_host: 6 x size FP64 Mandel eigenstress
+ * Submit one eigenstress solve (no reference counterpart; the reference
+ * solves it mode by mode, python/demo.py:24-40).  tau_host: 6 x size FP64 Mandel eigenstress
  * (copied at submit); the server owns the request until bri17_server_poll
  * returns it.  x_host: dim x size FP64, written with the solution when the
  * request finishes (must stay valid until then).  Returns the request id in
@@ -351,7 +355,7 @@ int bri17_server_submit(bri17_server* srv, const int* shape, const double* L,
                         int64_t* id);
 
 /*
- * Same, without the copy of tau at submit: tau_host is read when the request
+ * Same (no reference counterpart), without the copy of tau at submit: tau_host is read when the request
  * is admitted and must stay valid and unchanged until bri17_server_poll
  * returns the request.  With page-locked tau_host and x_host (cudaHostAlloc,
  * cudaHostRegister) the upload and the solution's download are asynchronous
@@ -365,17 +369,19 @@ int bri17_server_submit_borrowed(bri17_server* srv, const int* shape,
                                  double tol, int max_iterations, int64_t* id);
 
 /* Advance the server: admit, run one scheduling quantum, retire.  Returns
- * the number of active requests in *active. */
+ * the number of active requests in *active.  No reference counterpart. */
 int bri17_server_step(bri17_server* srv, int* active);
 
-/* Pop up to `cap` (>= 0) finished results; *count receives how many. */
+/* Pop up to `cap` (>= 0) finished results; *count receives how many.  No
+ * reference counterpart. */
 int bri17_server_poll(bri17_server* srv, bri17_request_result* out, int cap,
                       int* count);
 
-/* Cancel a queued or running request (its result reports CANCELLED). */
+/* Cancel a queued or running request (its result reports CANCELLED).  No
+ * reference counterpart. */
 int bri17_server_cancel(bri17_server* srv, int64_t id);
 
-/* Server clock (seconds since creation). */
+/* Server clock (seconds since creation).  No reference counterpart. */
 double bri17_server_clock(const bri17_server* srv);
 
 #ifdef __cplusplus
