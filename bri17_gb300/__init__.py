@@ -6,6 +6,6 @@ The compute path is the CUDA library ``libbri17_gb300.so`` (C ABI in
 ``include/bri17_gb300.h``); this package binds it.  ``pybri17`` re-exports
 the reference's Python module surface on top of it.
 """
-from .api import CartesianGrid, Hooke, version, wait_timeouts  # noqa: F401
+from .api import CartesianGrid, Hooke, set_wait_limit_ns, version, wait_timeouts  # noqa: F401
 
 __version__ = "0.1.0"

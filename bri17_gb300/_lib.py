@@ -26,6 +26,7 @@ STATUS = {
     0: "ok", 1: "invalid argument", 2: "unsupported size", 3: "CUDA error",
     4: "out of device memory", 5: "not converged", 6: "breakdown", 7: "no CUDA device",
     8: "busy", 9: "not found", 10: "cancelled",
+    11: "a bounded device wait ran out (results invalid)", 12: "residual stagnated",
 }
 F64, F32 = 0, 1
 CG_PLAIN, CG_MIXED, CG_MIXED_RESTART = 0, 1, 2
@@ -64,6 +65,9 @@ _SIGS = {
     "bri17_op_fused_form": ([vp, c_int_p], ctypes.c_int),
     "bri17_op_set_fused_form": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_wait_timeouts": ([c_int_p], ctypes.c_int),
+    "bri17_op_sync_status": ([vp, vp], ctypes.c_int),
+    "bri17_set_wait_limit_ns": ([ctypes.c_uint64], ctypes.c_int),
+    "bri17_server_inject_alloc_failure": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_op_set_float_pair": ([vp, ctypes.c_int], ctypes.c_int),
     "bri17_eigenstress_to_opposite_strain": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_op_set_pass_timing": ([vp, ctypes.c_int], ctypes.c_int),
@@ -73,6 +77,10 @@ _SIGS = {
     "bri17_modal_strain_displacement_batch": ([vp, vp, ctypes.c_int64, vp, vp], ctypes.c_int),
     "bri17_modal_eigenstress_to_opposite_strain_batch": (
         [vp, vp, ctypes.c_int64, vp, vp, vp], ctypes.c_int),
+    "bri17_modal_stiffness_host": ([vp, vp, ctypes.c_int64, vp], ctypes.c_int),
+    "bri17_modal_strain_displacement_host": ([vp, vp, ctypes.c_int64, vp], ctypes.c_int),
+    "bri17_modal_eigenstress_to_opposite_strain_host": (
+        [vp, vp, ctypes.c_int64, vp, vp], ctypes.c_int),
     "bri17_apply_stiffness": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_apply_stiffness_host": ([vp, vp, vp, vp], ctypes.c_int),
     "bri17_apply_stiffness_noalloc": ([ctypes.c_int, c_int_p, c_double_p, ctypes.c_double,

@@ -311,6 +311,12 @@ class Hooke:
             _stream_ptr(stream)), "bri17_eigenstress_to_opposite_strain")
         return eta
 
+    def sync_status(self, stream=None) -> int:
+        """Synchronise `stream` and return the handle's status: 0, or 11 when
+        a bounded device wait of its earlier work ran out (that work's
+        output is invalid); each failure is reported once."""
+        return _lib.load().bri17_op_sync_status(self._h, _stream_ptr(stream))
+
     def cg_solve(self, b, x0=None, tol: float = 1e-8, max_iterations: int = 100000,
                  mode: str = "plain", raise_on_failure: bool = True, stream=None):
         """Solve K x = b (zero-mean x) by CG.  b: FP64 CUDA tensor (DIM,
@@ -342,6 +348,14 @@ class Hooke:
         if rc != 0 and raise_on_failure:
             check(rc, "bri17_cg_solve")
         return x, out
+
+
+def set_wait_limit_ns(ns: int) -> None:
+    """Limit (ns of GPU global time) of the first wait on tile copies in the
+    tensor-copy kernels on the current device; 0 makes those waits give up
+    at once (diagnostics: tests of the failure path).  Default
+    1_000_000_000."""
+    check(_lib.load().bri17_set_wait_limit_ns(int(ns)), "bri17_set_wait_limit_ns")
 
 
 def wait_timeouts() -> int:

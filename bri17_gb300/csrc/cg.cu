@@ -149,6 +149,13 @@ __global__ void k_to_f32(float* __restrict__ out, const double* __restrict__ in,
     out[i] = (float)(in[i] * scale);
 }
 
+// a32 *= f.
+__global__ void k_scale_f32(float* __restrict__ a, float f, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] *= f;
+}
+
 // x64 += scale * d32.
 __global__ void k_add_f32(double* __restrict__ x, const float* __restrict__ d,
                           double scale, int64_t n) {
@@ -186,8 +193,9 @@ __global__ void __launch_bounds__(kRedThreads)
 // FP64 one (aux = its squared norm); keep the search direction, resume.
 // At least one more chunk runs even when the replaced residual already meets
 // the FP32 threshold, so every update changes the iterate.
-__global__ void k_reliable_resume(CgState* st) {
+__global__ void k_reliable_resume(CgState* st, double thresh) {
   st->rr = st->aux;
+  st->thresh = thresh;
   st->flag = BRI17_OK;
   st->pause = 0;
   st->active = isfinite(st->aux) ? 1 : 0;
@@ -341,6 +349,11 @@ static int run_cg(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
   while (w->st_host->active && w->st_host->iters < budget) {
     BRI17_CUDA_TRY(cudaGraphLaunch(*exec, w->stream));
     BRI17_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    const int ts = take_status(opk);  // a bounded device wait of the chunk ran out
+    if (ts != BRI17_OK) {
+      *iters = w->st_host->iters;
+      return ts;
+    }
   }
   *iters = w->st_host->iters;
   if (w->st_host->flag != BRI17_OK) return w->st_host->flag;
@@ -420,8 +433,10 @@ static int solve_plain64(bri17_op* op, const double* b, double* x, double tol,
   info->outer_iterations = 1;
   info->rel_residual = sqrt(w->st_host->aux / bb);
   if (status == BRI17_OK && !(info->rel_residual <= tol * 1.0000001 + 1e-300)) {
-    // The recursive residual met tol but the recomputed one did not.
-    status = BRI17_ERR_NOT_CONVERGED;
+    // The recursive residual met tol but the recomputed one did not: the
+    // true residual has stagnated at the accuracy rounding allows.
+    set_error("the recursive CG residual met tol but the recomputed FP64 residual did not");
+    status = BRI17_ERR_STAGNATED;
   }
   info->status = status;
   BRI17_CUDA_TRY(cudaMemcpyAsync(x, w->x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -567,6 +582,10 @@ static int solve_mixed(bri17_op* op, const double* b, double* x, double tol,
                            &w->epoch32, maxit - total, &iters);
     total += iters;
     if (st == BRI17_ERR_CUDA || st == BRI17_ERR_OUT_OF_MEMORY) return st;
+    if (st == BRI17_ERR_TIMEOUT) {  // the FP32 correction is invalid: not folded in
+      status = st;
+      break;
+    }
     if (st == BRI17_ERR_BREAKDOWN && iters == 0) {
       status = BRI17_ERR_BREAKDOWN;
       break;
@@ -591,6 +610,7 @@ static int solve_mixed(bri17_op* op, const double* b, double* x, double tol,
 static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double tol,
                                 int maxit, bri17_cg_info* info) {
   constexpr double kDelta = 0.1;
+  constexpr int kStallUpdates = 4;
   if (op->precision != BRI17_F64) {
     set_error("mixed-precision CG needs an FP64 handle");
     return BRI17_ERR_INVALID_ARGUMENT;
@@ -645,17 +665,24 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
   int status = BRI17_ERR_NOT_CONVERGED;
   if (rel <= tol) status = BRI17_OK;
   if (status != BRI17_OK) {
-    k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0, n);
+    // The FP32 vectors carry the residual scaled to unit norm (r32 = r / sig,
+    // d32 and p32 in the same units), so that their products stay far from
+    // FP32 underflow however small the FP64 residual gets.
+    double sig = sqrt(rr64);
+    k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0 / sig, n);
     BRI17_CUDA_TRY(cudaMemsetAsync(w->d32, 0, n * sizeof(float), s));
-    // aux = b.b so that k_start's threshold is tol^2 b.b.
+    // aux = b.b, so that k_start's threshold is tol^2 b.b / sig^2 (the
+    // stopping test in the scaled units).
     k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
     k_start<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->p32, n, w->st, w->partials,
-                                             tol * tol);
+                                             tol * tol / rr64);
     rc = get_graph<float>(op32, w, w->d32, w->r32, w->p32, w->q32, &w->graph32, &w->epoch32);
     if (rc != BRI17_OK) return rc;
     rc = read_state(w);
     if (rc != BRI17_OK) return rc;
     double rmax2 = rr64;  // squared norm at the last reliable update
+    double best2 = rr64;  // smallest squared FP64 residual so far
+    int stalled = 0;      // consecutive reliable updates that did not halve it
     int total = 0;
     int breakdowns = 0;  // consecutive FP32 breakdowns (p.Kp <= 0 or NaN)
     while (true) {
@@ -663,6 +690,12 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
       BRI17_CUDA_TRY(cudaStreamSynchronize(s));
       const CgState h = *w->st_host;
       total = h.iters;
+      if (take_status(op) != BRI17_OK) {
+        // A bounded device wait of the chunk ran out: its FP32 work is
+        // invalid; the FP64 iterate is kept as it was at the last update.
+        status = BRI17_ERR_TIMEOUT;
+        break;
+      }
       if (h.flag != BRI17_OK) {
         // An FP32 breakdown is answered by a reliable update; two in a row
         // without progress end the solve.
@@ -673,11 +706,11 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
       } else {
         breakdowns = 0;
       }
-      const bool dropped = h.rr < kDelta * kDelta * rmax2;
+      const bool dropped = h.rr * sig * sig < kDelta * kDelta * rmax2;
       const bool budget = total >= maxit;
       if (!(dropped || !h.active || budget)) continue;
-      // Reliable update: x += d (FP64), r = b - K x (FP64), r32 = r.
-      k_add_f32<<<grid1(n), 256, 0, s>>>(w->x, w->d32, 1.0, n);
+      // Reliable update: x += sig d (FP64), r = b - K x (FP64), r32 = r / sig'.
+      k_add_f32<<<grid1(n), 256, 0, s>>>(w->x, w->d32, sig, n);
       BRI17_CUDA_TRY(cudaMemsetAsync(w->d32, 0, n * sizeof(float), s));
       rc = true_residual(&rr64);
       if (rc != BRI17_OK) return rc;
@@ -695,10 +728,25 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
         status = BRI17_ERR_NOT_CONVERGED;
         break;
       }
+      // Stagnation: each update follows a 10x drop of the FP32 residual, so
+      // the FP64 one falls by about as much while it can; kStallUpdates
+      // updates in a row that do not halve the best FP64 residual mean that
+      // tol lies below what the FP64 residual computation resolves.
+      if (rr64 < 0.25 * best2) {
+        best2 = rr64;
+        stalled = 0;
+      } else if (++stalled >= kStallUpdates) {
+        set_error("the FP64 residual stopped decreasing above tol");
+        status = BRI17_ERR_STAGNATED;
+        break;
+      }
       rmax2 = rr64;
-      k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0, n);
+      const double sig_new = sqrt(rr64);
+      k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0 / sig_new, n);
+      k_scale_f32<<<grid1(n), 256, 0, s>>>(w->p32, (float)(sig / sig_new), n);
+      sig = sig_new;
       k_dot<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->r32, n, w->st, w->partials);
-      k_reliable_resume<<<1, 1, 0, s>>>(w->st);
+      k_reliable_resume<<<1, 1, 0, s>>>(w->st, tol * tol * bb / rr64);
       rc = read_state(w);
       if (rc != BRI17_OK) return rc;
       if (!w->st_host->active) {
@@ -738,6 +786,8 @@ extern "C" int bri17_cg_solve(bri17_op* op, const double* b, double* x,
   if (dc != BRI17_OK) return info->status = dc;
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return info->status = cuda_fail(e, "cudaStreamSynchronize");
+  const int ts = take_status(op);  // a failure of earlier work on the handle
+  if (ts != BRI17_OK) return info->status = ts;
   int rc;
   if (mode == BRI17_CG_MIXED)
     rc = solve_mixed_reliable(op, b, x, tol, max_iterations, info);

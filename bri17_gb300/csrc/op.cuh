@@ -39,6 +39,20 @@ struct bri17_op {
   int fused_form_df;
   void* table_df;
   bri17gb::Tables<bri17gb::df64> tabdf;
+  // Status words the handle's kernels set when a bounded device wait runs
+  // out ([0]) or a tile is skipped ([1]): page-locked host memory mapped
+  // into the device, read by the host without a copy.
+  int* status_host;
+  int* status_dev;
+  // Per-mode calls on host buffers (bri17_modal_*_host, lazy): page-locked
+  // staging mapped into the device, so a call is one kernel launch and one
+  // synchronisation of a private stream; a lock, because those calls are
+  // const in the C++ API and may come from several threads.
+  unsigned char* mode_stage_host;
+  unsigned char* mode_stage_dev;
+  size_t mode_stage_bytes;
+  cudaStream_t mode_stream;
+  std::mutex* mode_mu;
 };
 
 namespace bri17gb {
@@ -52,6 +66,13 @@ inline size_t scalar_bytes(const bri17_op* op) {
 
 // BRI17_OK when the current CUDA device is the handle's device.
 int check_device(const bri17_op* op);
+
+// BRI17_ERR_TIMEOUT, with the status words cleared, when one of the handle's
+// kernels (or its FP32 twin's) recorded a bounded device wait that ran out,
+// or a skipped tile, since the last call; else BRI17_OK.  Reads completed
+// work only: call it after synchronising the streams the work ran on, or at
+// entry to report an earlier call's failure.
+int take_status(bri17_op* op);
 
 // Grow the spectrum buffer to `comps` components.
 int ensure_spectrum(bri17_op* op, int comps);

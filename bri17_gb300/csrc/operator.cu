@@ -48,6 +48,25 @@ int check_device(const bri17_op* op) {
   return BRI17_OK;
 }
 
+int take_status(bri17_op* op) {
+  int rc = BRI17_OK;
+  for (bri17_op* o : {op, op->twin32}) {
+    if (!o || !o->status_host) continue;
+    // Host atomics: a kernel's store that lands after the exchange is kept
+    // for the next check.
+    const int timeout = __atomic_exchange_n(&o->status_host[0], 0, __ATOMIC_SEQ_CST);
+    const int skipped = __atomic_exchange_n(&o->status_host[1], 0, __ATOMIC_SEQ_CST);
+    if (timeout || skipped) {
+      set_error(timeout ? "a bounded device wait on tile copies ran out: the output of the "
+                          "operator work it belonged to is invalid"
+                        : "a tile was skipped (misplaced shared-memory window): the output of "
+                          "the operator work it belonged to is invalid");
+      rc = BRI17_ERR_TIMEOUT;
+    }
+  }
+  return rc;
+}
+
 // ---------------------------------------------------------------------------
 // Plans.
 
@@ -548,6 +567,7 @@ static FusedParams<T> fused_params(const bri17_op* op, const Tables<T>& tab,
                                                         : (T)op->corr;
   fp.mat = nullptr;
   fp.form = op->fused_form;
+  fp.status = op->status_dev;
   return fp;
 }
 
@@ -1029,6 +1049,8 @@ extern "C" const char* bri17_status_string(int s) {
     case BRI17_ERR_BUSY: return "busy";
     case BRI17_ERR_NOT_FOUND: return "not found";
     case BRI17_ERR_CANCELLED: return "cancelled";
+    case BRI17_ERR_TIMEOUT: return "a bounded device wait ran out (results invalid)";
+    case BRI17_ERR_STAGNATED: return "residual stagnated above the tolerance";
     default: return "unknown status";
   }
 }
@@ -1118,8 +1140,19 @@ extern "C" int bri17_op_create(int dim, const int* shape, const double* L,
     delete op;
     return cuda_fail(e, "cudaMemcpy(tables)");
   }
+  e = cudaHostAlloc((void**)&op->status_host, 4 * sizeof(int), cudaHostAllocMapped);
+  if (e == cudaSuccess)
+    e = cudaHostGetDevicePointer((void**)&op->status_dev, op->status_host, 0);
+  if (e != cudaSuccess) {
+    cudaFreeHost(op->status_host);
+    cudaFree(op->table_mem);
+    delete op;
+    return cuda_fail(e, "cudaHostAlloc(status words)");
+  }
+  memset(op->status_host, 0, 4 * sizeof(int));
   rc = ensure_spectrum(op, dim);
   if (rc != BRI17_OK) {
+    cudaFreeHost(op->status_host);
     cudaFree(op->table_mem);
     delete op;
     return rc;
@@ -1130,6 +1163,7 @@ extern "C" int bri17_op_create(int dim, const int* shape, const double* L,
   else
     set_smem_attrs<float>();
   if (precision == BRI17_F32 && g.use_p8[0]) autotune_fused_form(op);
+  op->mode_mu = new std::mutex();
   *out = op;
   return BRI17_OK;
 }
@@ -1149,6 +1183,10 @@ extern "C" int bri17_op_destroy(bri17_op* op) {
   }
   if (op->cg_work && op->cg_free) op->cg_free(op->cg_work);
   delete reinterpret_cast<PassTiming*>(op->timing);
+  cudaFreeHost(op->status_host);
+  cudaFreeHost(op->mode_stage_host);
+  if (op->mode_stream) cudaStreamDestroy(op->mode_stream);
+  delete op->mode_mu;
   delete op;
   return BRI17_OK;
 }
@@ -1224,6 +1262,98 @@ extern "C" int bri17_modal_eigenstress_to_opposite_strain_batch(
       a, k, n, (const double2*)tau, (double2*)eta);
   BRI17_CUDA_TRY(cudaGetLastError());
   return BRI17_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Per-mode functions on host buffers.
+
+namespace bri17gb {
+
+// Runs launch(k_dev, in_dev, out_dev, stream) on the handle's private stream
+// over page-locked staging mapped into the device: k (n x dim int32) and
+// `in` are copied into the staging, the kernel reads and writes it in
+// place (over the host link), and `out` is copied back once the stream has
+// synchronised.  No device allocation after the first call of a given size.
+template <typename Launch>
+static int modal_host_call(const bri17_op* cop, const int* k, int64_t n, const void* in,
+                           size_t in_bytes, void* out, size_t out_bytes, Launch&& launch) {
+  bri17_op* op = const_cast<bri17_op*>(cop);
+  std::lock_guard<std::mutex> lock(*op->mode_mu);
+  const size_t k_bytes = align16((size_t)n * op->g.dim * sizeof(int));
+  const size_t need = k_bytes + align16(in_bytes) + out_bytes;
+  if (op->mode_stage_bytes < need) {
+    cudaFreeHost(op->mode_stage_host);
+    op->mode_stage_host = op->mode_stage_dev = nullptr;
+    op->mode_stage_bytes = 0;
+    const size_t bytes = std::max<size_t>(need, 4096);
+    BRI17_CUDA_TRY(cudaHostAlloc((void**)&op->mode_stage_host, bytes, cudaHostAllocMapped));
+    BRI17_CUDA_TRY(cudaHostGetDevicePointer((void**)&op->mode_stage_dev, op->mode_stage_host, 0));
+    op->mode_stage_bytes = bytes;
+  }
+  if (!op->mode_stream)
+    BRI17_CUDA_TRY(cudaStreamCreateWithFlags(&op->mode_stream, cudaStreamNonBlocking));
+  memcpy(op->mode_stage_host, k, (size_t)n * op->g.dim * sizeof(int));
+  if (in_bytes) memcpy(op->mode_stage_host + k_bytes, in, in_bytes);
+  unsigned char* d = op->mode_stage_dev;
+  launch((const int*)d, (const void*)(d + k_bytes), (void*)(d + k_bytes + align16(in_bytes)),
+         op->mode_stream);
+  BRI17_CUDA_TRY(cudaGetLastError());
+  BRI17_CUDA_TRY(cudaStreamSynchronize(op->mode_stream));
+  memcpy(out, op->mode_stage_host + k_bytes + align16(in_bytes), out_bytes);
+  return BRI17_OK;
+}
+
+static int modal_host_checks(const bri17_op* op, const int* k, int64_t n, const void* out) {
+  if (!op) return invalid("null handle");
+  const int dc = check_device(op);
+  if (dc != BRI17_OK) return dc;
+  if (n < 0) return invalid("negative count");
+  if (n > 0 && (!k || !out)) return invalid("null pointer");
+  return BRI17_OK;
+}
+
+}  // namespace bri17gb
+
+extern "C" int bri17_modal_stiffness_host(const bri17_op* op, const int* k, int64_t n,
+                                          void* K) {
+  int rc = modal_host_checks(op, k, n, K);
+  if (rc != BRI17_OK || n == 0) return rc;
+  const ModalArgs a = modal_args(op);
+  const int d2 = op->g.dim * op->g.dim;
+  return modal_host_call(op, k, n, nullptr, 0, K, (size_t)n * d2 * sizeof(double2),
+                         [&](const int* kd, const void*, void* o, cudaStream_t st) {
+                           modal_stiffness_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                               a, kd, n, (double2*)o);
+                         });
+}
+
+extern "C" int bri17_modal_strain_displacement_host(const bri17_op* op, const int* k,
+                                                    int64_t n, void* B) {
+  int rc = modal_host_checks(op, k, n, B);
+  if (rc != BRI17_OK || n == 0) return rc;
+  const ModalArgs a = modal_args(op);
+  return modal_host_call(op, k, n, nullptr, 0, B, (size_t)n * op->g.dim * sizeof(double2),
+                         [&](const int* kd, const void*, void* o, cudaStream_t st) {
+                           modal_strain_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                               a, kd, n, (double2*)o);
+                         });
+}
+
+extern "C" int bri17_modal_eigenstress_to_opposite_strain_host(const bri17_op* op,
+                                                               const int* k, int64_t n,
+                                                               const void* tau, void* eta) {
+  int rc = modal_host_checks(op, k, n, eta);
+  if (rc != BRI17_OK || n == 0) return rc;
+  if (!tau) return invalid("null pointer");
+  const ModalArgs a = modal_args(op);
+  const int sym = op->g.dim == 2 ? 3 : 6;
+  const size_t bytes = (size_t)n * sym * sizeof(double2);
+  return modal_host_call(op, k, n, tau, bytes, eta, bytes,
+                         [&](const int* kd, const void* t, void* o, cudaStream_t st) {
+                           modal_eigenstress_kernel<<<(unsigned)((n + 127) / 128), 128, 0,
+                                                      st>>>(a, kd, n, (const double2*)t,
+                                                            (double2*)o);
+                         });
 }
 
 // ---------------------------------------------------------------------------
@@ -1392,6 +1522,10 @@ extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,
     const int dc = check_device(op);
     if (dc != BRI17_OK) return dc;
   }
+  {
+    const int ts = take_status(op);  // a failure of earlier work on the handle
+    if (ts != BRI17_OK) return ts;
+  }
   if (!u || !f) return invalid("null pointer");
   if (op->float_pair) {
     const int rc = ensure_spectrum(op, op->g.dim);
@@ -1515,6 +1649,10 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
     const int dc = check_device(op);
     if (dc != BRI17_OK) return dc;
   }
+  {
+    const int ts = take_status(op);  // a failure of earlier work on the handle
+    if (ts != BRI17_OK) return ts;
+  }
   if (!u_host || !f_host) return invalid("null pointer");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t bytes = (size_t)op->g.dim * op->g.size * scalar_bytes(op);
@@ -1556,7 +1694,7 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
                                                op->spec, nullptr, st);
     if (rc != BRI17_OK) return rc;
     BRI17_CUDA_TRY(cudaStreamSynchronize(st));
-    return BRI17_OK;
+    return take_status(op);
   }
   if (op->float_pair) {
     // Pageable buffers: whole-field copies around the float-pair passes.
@@ -1567,11 +1705,14 @@ extern "C" int bri17_apply_stiffness_host(bri17_op* op, const void* u_host,
     if (rc != BRI17_OK) return rc;
     BRI17_CUDA_TRY(cudaMemcpyAsync(f_host, op->stage_out, bytes, cudaMemcpyDeviceToHost, st));
     BRI17_CUDA_TRY(cudaStreamSynchronize(st));
-    return BRI17_OK;
+    return take_status(op);
   }
   if (op->precision == BRI17_F64)
-    return apply_host_pipelined<double>(op, (const double*)u_host, (double*)f_host, st);
-  return apply_host_pipelined<float>(op, (const float*)u_host, (float*)f_host, st);
+    rc = apply_host_pipelined<double>(op, (const double*)u_host, (double*)f_host, st);
+  else
+    rc = apply_host_pipelined<float>(op, (const float*)u_host, (float*)f_host, st);
+  if (rc != BRI17_OK) return rc;
+  return take_status(op);
 }
 
 extern "C" int bri17_apply_strain(bri17_op* op, const void* u, void* eps,
@@ -1580,6 +1721,10 @@ extern "C" int bri17_apply_strain(bri17_op* op, const void* u, void* eps,
   {
     const int dc = check_device(op);
     if (dc != BRI17_OK) return dc;
+  }
+  {
+    const int ts = take_status(op);  // a failure of earlier work on the handle
+    if (ts != BRI17_OK) return ts;
   }
   if (!u || !eps) return invalid("null pointer");
   const int sym = op->g.dim == 2 ? 3 : 6;
@@ -1600,6 +1745,10 @@ extern "C" int bri17_eigenstress_rhs(bri17_op* op, const void* tau, void* b,
     const int dc = check_device(op);
     if (dc != BRI17_OK) return dc;
   }
+  {
+    const int ts = take_status(op);  // a failure of earlier work on the handle
+    if (ts != BRI17_OK) return ts;
+  }
   if (!tau || !b) return invalid("null pointer");
   const int sym = op->g.dim == 2 ? 3 : 6;
   int rc = ensure_spectrum(op, sym);
@@ -1613,6 +1762,10 @@ extern "C" int bri17_eigenstress_to_opposite_strain(bri17_op* op, const void* ta
   {
     const int dc = check_device(op);
     if (dc != BRI17_OK) return dc;
+  }
+  {
+    const int ts = take_status(op);  // a failure of earlier work on the handle
+    if (ts != BRI17_OK) return ts;
   }
   if (!tau || !eta) return invalid("null pointer");
   const int sym = op->g.dim == 2 ? 3 : 6;
@@ -1649,6 +1802,23 @@ extern "C" int bri17_wait_timeouts(int* count) {
   if (e == cudaSuccess) e = tma_wait_timeouts_df(&b);
   if (e != cudaSuccess) return cuda_fail(e, "reading the wait-timeout count");
   *count = a + b;
+  return BRI17_OK;
+}
+
+extern "C" int bri17_op_sync_status(bri17_op* op, void* stream) {
+  if (!op) return invalid("null handle");
+  {
+    const int dc = check_device(op);
+    if (dc != BRI17_OK) return dc;
+  }
+  BRI17_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return take_status(op);
+}
+
+extern "C" int bri17_set_wait_limit_ns(uint64_t ns) {
+  cudaError_t e = tma_set_wait_limit_f32(ns);
+  if (e == cudaSuccess) e = tma_set_wait_limit_df(ns);
+  if (e != cudaSuccess) return cuda_fail(e, "setting the device wait limit");
   return BRI17_OK;
 }
 

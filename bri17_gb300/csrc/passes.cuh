@@ -51,6 +51,7 @@ struct FusedParams {
   T corr;           // normalisation of strain / rhs modes
   const T* mat;     // optional per-batch (s, mu) pairs, overriding s, mu
   int form;         // power-of-two axis-0 stiffness pass: 0 registers, 1 staged
+  int* status;      // the handle's status words (mapped host memory) or null
 };
 
 // ---------------------------------------------------------------------------

@@ -28,6 +28,11 @@ void ct_set_smem_attrs_df_axis0(size_t max_smem) {
   ct_set_smem_attrs_tma<df64, false>(max_smem);
 }
 
+cudaError_t tma_set_wait_limit_df(uint64_t ns) {
+  const unsigned long long v = ns;
+  return cudaMemcpyToSymbol(g_tma_wait_limit_ns, &v, sizeof(v));
+}
+
 cudaError_t tma_wait_timeouts_df(int* count) {
   int n = 0;
   cudaError_t e = cudaMemcpyFromSymbol(&n, g_tma_timeouts, sizeof(int));

@@ -14,6 +14,11 @@ bool ct_axis0_stiffness_tma_f32(int n0, bool keep, cplx<float>* X, int64_t P, in
 
 void ct_set_smem_attrs_tma_f32(size_t max_smem) { ct_set_smem_attrs_tma<float>(max_smem); }
 
+cudaError_t tma_set_wait_limit_f32(uint64_t ns) {
+  const unsigned long long v = ns;
+  return cudaMemcpyToSymbol(g_tma_wait_limit_ns, &v, sizeof(v));
+}
+
 cudaError_t tma_wait_timeouts_f32(int* count) {
   int n = 0;
   cudaError_t e = cudaMemcpyFromSymbol(&n, g_tma_timeouts, sizeof(int));

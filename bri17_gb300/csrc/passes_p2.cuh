@@ -443,6 +443,8 @@ __global__ void __launch_bounds__(kP2Threads)
 
 // Bounded mbarrier waits that ran out in this translation unit's TMA kernels.
 static __device__ int g_tma_timeouts;
+// Limit of the first wait on a tile's copies (ns of global time).
+static __device__ unsigned long long g_tma_wait_limit_ns = kWaitLimitNs;
 
 // Axis 0, fused stiffness, TMA-staged (3D): the CTA's tile -- TB consecutive
 // lines of all DIM components, n0 rows each, laid out [c][k0][line] in shared
@@ -484,7 +486,10 @@ __global__ void __launch_bounds__(256)
   // The copy destinations must be 128-byte aligned; the launch guarantees
   // it, and a misplaced window skips the CTA with an error count.
   if (smem_addr(tile) & 127u) {
-    if (threadIdx.x == 0) atomicAdd(&g_tma_timeouts, 1);
+    if (threadIdx.x == 0) {
+      atomicAdd(&g_tma_timeouts, 1);
+      report_status(fp.status, 1);
+    }
     return;
   }
   __syncthreads();
@@ -510,14 +515,17 @@ __global__ void __launch_bounds__(256)
   const T phi2 = ldg_val(fp.tab.kphi[2] + k2), chi2 = ldg_val(fp.tab.kchi[2] + k2),
           psi2 = ldg_val(fp.tab.kpsi[2] + k2);
   const LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
-  // One second of global time per wait; a wait that runs out is counted,
-  // the tile is neither transformed nor stored, and the CTA waits (bounded
-  // again) for its copies before leaving.
-  const bool arrived = mbar_wait(bar, 0, 1000000000ull);
+  // One second of global time per wait (g_tma_wait_limit_ns); a wait that
+  // runs out is counted and reported to the handle, the tile is neither
+  // transformed nor stored, and the CTA waits (bounded again, by
+  // kWaitLimitNs) for its copies to land before leaving, so that no copy
+  // writes shared memory after the CTA has left.
+  const bool arrived = mbar_wait(bar, 0, g_tma_wait_limit_ns);
   if (__syncthreads_or(!arrived)) {
     if (threadIdx.x == 0) {
       atomicAdd(&g_tma_timeouts, 1);
-      mbar_wait(bar, 0, 1000000000ull);
+      report_status(fp.status, 0);
+      mbar_wait(bar, 0, kWaitLimitNs);
     }
     return;
   }

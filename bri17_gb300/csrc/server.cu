@@ -340,6 +340,10 @@ struct bri17_server {
   std::vector<bri17_request_result> done;
   std::unordered_map<int64_t, Request*> live;
   std::vector<Request*> finishing;  // solution copies to page-locked x_host in flight
+  // Fault injection (bri17_server_inject_alloc_failure): when >= 0, the next
+  // bucket creation fails at its work buffer number fail_alloc_at (0-based)
+  // as cudaMalloc does when memory runs out.
+  int fail_alloc_at = -1;
   std::chrono::steady_clock::time_point t0;
   double now() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -442,10 +446,15 @@ int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
   if (rc != BRI17_OK) return fail(rc);
   const int64_t n = B->n, Sn = S * n;
   const int64_t cspec = B->op32->g.cspec;
-#define ALLOC(p, bytes_)                                                   \
-  do {                                                                     \
-    cudaError_t _e = cudaMalloc((void**)&(p), (bytes_));                   \
-    if (_e != cudaSuccess) return fail(cuda_fail(_e, "cudaMalloc(bucket)")); \
+  // An injected failure takes the place of work buffer number inject_at.
+  const int inject_at = srv->fail_alloc_at;
+  srv->fail_alloc_at = -1;
+  int alloc_no = 0;
+#define ALLOC(p, bytes_)                                                            \
+  do {                                                                              \
+    cudaError_t _e = alloc_no++ == inject_at ? cudaErrorMemoryAllocation             \
+                                             : cudaMalloc((void**)&(p), (bytes_));  \
+    if (_e != cudaSuccess) return fail(cuda_fail(_e, "cudaMalloc(bucket)"));        \
   } while (0)
   ALLOC(B->b, Sn * 8);
   ALLOC(B->x, Sn * 8);
@@ -678,6 +687,15 @@ extern "C" int bri17_server_set_size_priority(bri17_server* srv, int enable) {
   return BRI17_OK;
 }
 
+extern "C" int bri17_server_inject_alloc_failure(bri17_server* srv, int at) {
+  if (!srv || at < -1) {
+    set_error("null server or allocation number below -1");
+    return BRI17_ERR_INVALID_ARGUMENT;
+  }
+  srv->fail_alloc_at = at;
+  return BRI17_OK;
+}
+
 extern "C" int bri17_server_destroy(bri17_server* srv) {
   if (!srv) return BRI17_OK;
   for (Bucket* B : srv->buckets) free_bucket(B);
@@ -878,6 +896,21 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
     if (qs != cudaSuccess) return cuda_fail(qs, "server chunk");
     B->in_flight = false;
     progress = true;
+    if (take_status(B->op32) != BRI17_OK) {
+      // A bounded device wait of the chunk ran out: the chunk's FP32 work is
+      // invalid for every slot that was iterating; those requests fail.
+      for (int z = 0; z < B->S; z++) {
+        if (B->slot_state[z] != kInner) continue;
+        ks_set_inactive<<<1, 1, 0, B->stream>>>(B->st + z);
+        Request* q = B->slot_req[z];
+        q->iters = B->st_host[z].iters;
+        q->rel = NAN;
+        B->slot_state[z] = kFree;
+        B->slot_req[z] = nullptr;
+        finish(srv, q, BRI17_ERR_TIMEOUT);
+        B->enqueued = true;
+      }
+    }
     const int rc = retire(srv, B);
     if (rc != BRI17_OK) return rc;
   }
@@ -905,6 +938,16 @@ extern "C" int bri17_server_step(bri17_server* srv, int* active) {
       }
       if (rc == BRI17_ERR_BUSY) {
         ++it;
+        continue;
+      }
+      if (rc == BRI17_ERR_OUT_OF_MEMORY || rc == BRI17_ERR_UNSUPPORTED_SIZE ||
+          rc == BRI17_ERR_INVALID_ARGUMENT) {
+        // The request cannot get a bucket: it fails alone; the requests in
+        // flight are untouched (make_bucket released what it had built).
+        cudaGetLastError();
+        it = srv->queue.erase(it);
+        progress = true;
+        finish(srv, q, rc);
         continue;
       }
       if (rc != BRI17_OK) return rc;

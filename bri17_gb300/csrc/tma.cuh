@@ -48,8 +48,11 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
 }
 
 // Waits for phase `parity` of the barrier; gives up after `limit_ns`
-// nanoseconds of global time and returns false.
+// nanoseconds of global time and returns false.  A limit of 0 gives up at
+// once, without looking at the barrier (a diagnostic setting that makes the
+// failure path run).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+  if (limit_ns == 0) return false;
   const uint32_t a = smem_addr(bar);
   uint64_t t0 = 0;
   for (uint32_t it = 0;; it++) {
@@ -64,6 +67,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
     if (done) return true;
     if (it == 0) t0 = global_timer_ns();
     else if (global_timer_ns() - t0 > limit_ns) return false;
+  }
+}
+
+// Default limit of a bounded wait on tile copies: one second of global time.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+// A kernel's report of a failed bounded wait: status[0] is set when a wait
+// on tile copies ran out, status[1] when a tile was skipped because its
+// shared-memory window was misplaced.  `status` points at page-locked host
+// memory mapped into the device (the handle's status words; may be null),
+// so the host reads it without a copy; kernels only ever store 1.
+__device__ __forceinline__ void report_status(int* status, int which) {
+  if (status) {
+    *reinterpret_cast<volatile int*>(status + which) = 1;
+    __threadfence_system();
   }
 }
 
@@ -110,5 +128,11 @@ bool encode_tiled_map_3d(CUtensorMap* map, const void* base, int elem_bytes, uin
 // (read and cleared on the current device).
 cudaError_t tma_wait_timeouts_f32(int* count);
 cudaError_t tma_wait_timeouts_df(int* count);
+// Limit of the first bounded wait on tile copies in those kernels, on the
+// current device (diagnostics; kWaitLimitNs by default).  The wait that
+// follows a run-out one, for the CTA's own copies in flight, keeps
+// kWaitLimitNs.
+cudaError_t tma_set_wait_limit_f32(uint64_t ns);
+cudaError_t tma_set_wait_limit_df(uint64_t ns);
 
 }  // namespace bri17gb

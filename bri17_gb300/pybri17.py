@@ -19,13 +19,23 @@ Beyond the reference, every Hooke class carries the batched and whole-field
 methods of :class:`bri17_gb300.api.Hooke` (``modal_stiffness_batch``,
 ``apply_stiffness``, ``apply_strain``, ``eigenstress_rhs``, ``cg_solve``),
 which remove the per-mode Python round trip of python/demo.py:34-40.
-The per-mode methods run the same CUDA kernels with a batch of one.
+The per-mode methods run the same CUDA kernels with a batch of one, through
+the host-buffer entry points (bri17_modal_*_host): the caller's numpy arrays
+are staged in page-locked memory the handle keeps, one kernel runs, and the
+result is written into the caller's array -- no device allocation or torch
+round trip per call.
+
+``import pybri17`` (the reference's module name) finds this module through
+the top-level ``pybri17.py`` beside this package.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
-from . import api
+from . import _lib, api
+from ._lib import check
 
 __author__ = "S. Brisard"
 __version__ = "0.1"
@@ -81,27 +91,49 @@ class _HookeBase(api.Hooke):
         # The reference copies the grid (include/bri17/bri17.hpp:193-194).
         super().__init__(mu, nu, type(grid)(grid.shape, grid.L), precision="f64")
 
-    def modal_strain_displacement(self, k, B):
-        _check_contiguous(B, np.complex128)
+    def _k(self, k):
         k = np.asarray(k, dtype=np.intc)
         _check_contiguous(k, np.intc)
-        out = self.modal_strain_displacement_batch(k.reshape(1, self._DIM))
-        B[: self._DIM] = out.cpu().numpy().reshape(-1)
+        if k.shape[0] < self._DIM:
+            raise ValueError(f"expected {self._DIM} frequency indices")
+        return k
+
+    @staticmethod
+    def _room(a, n):
+        if a.shape[0] < n:
+            raise ValueError(f"expected an array of at least {n} entries")
+
+    def modal_strain_displacement(self, k, B):
+        _check_contiguous(B, np.complex128)
+        k = self._k(k)
+        self._room(B, self._DIM)
+        check(_lib.load().bri17_modal_strain_displacement_host(
+            self.handle, k.ctypes.data_as(ctypes.c_void_p), 1,
+            B.ctypes.data_as(ctypes.c_void_p)), "bri17_modal_strain_displacement_host")
 
     def modal_stiffness_matrix(self, k, K):
         _check_contiguous(K, np.complex128)
-        k = np.asarray(k, dtype=np.intc)
-        _check_contiguous(k, np.intc)
-        out = self.modal_stiffness_batch(k.reshape(1, self._DIM))
-        K[: self._DIM * self._DIM] = out.cpu().numpy().reshape(-1)
+        k = self._k(k)
+        self._room(K, self._DIM * self._DIM)
+        check(_lib.load().bri17_modal_stiffness_host(
+            self.handle, k.ctypes.data_as(ctypes.c_void_p), 1,
+            K.ctypes.data_as(ctypes.c_void_p)), "bri17_modal_stiffness_host")
 
     def modal_eigenstress_to_opposite_strain(self, k, tau, eta):
         _check_contiguous(tau, np.complex128)
         _check_contiguous(eta, np.complex128)
         sym = 3 if self._DIM == 2 else 6
-        k = np.asarray(k, dtype=np.intc).reshape(1, self._DIM)
-        out = self.modal_eigenstress_to_opposite_strain_batch(k, tau[:sym].reshape(1, sym))
-        eta[:sym] = out.cpu().numpy().reshape(-1)
+        # The reference does not check k here (python/pybri17.cpp:91-92); it
+        # is read as DIM int32 values.
+        k = np.ascontiguousarray(np.asarray(k, dtype=np.intc).reshape(-1)[: self._DIM])
+        if k.shape[0] < self._DIM:
+            raise ValueError(f"expected {self._DIM} frequency indices")
+        self._room(tau, sym)
+        self._room(eta, sym)
+        check(_lib.load().bri17_modal_eigenstress_to_opposite_strain_host(
+            self.handle, k.ctypes.data_as(ctypes.c_void_p), 1,
+            tau.ctypes.data_as(ctypes.c_void_p), eta.ctypes.data_as(ctypes.c_void_p)),
+            "bri17_modal_eigenstress_to_opposite_strain_host")
 
 
 class Hooke2f64(_HookeBase):

@@ -124,6 +124,14 @@ class Server:
     def result(self, rid: int) -> np.ndarray:
         return self._out.pop(rid)[1]
 
+    def inject_alloc_failure(self, at: int) -> None:
+        """Fault injection: the next bucket creation fails at its work
+        buffer number `at` as if device memory had run out (-1 cancels);
+        the request that needed the bucket finishes with status 4 (out of
+        memory) and the others are unaffected."""
+        check(_lib.load().bri17_server_inject_alloc_failure(self._h, int(at)),
+              "bri17_server_inject_alloc_failure")
+
     def cancel(self, rid: int) -> int:
         return _lib.load().bri17_server_cancel(self._h, int(rid))
 

@@ -38,15 +38,6 @@ inline void check(int status, const char* where) {
   throw std::runtime_error(msg);
 }
 
-// Device scratch for one per-mode call (k, inputs and outputs of a batch of
-// one mode).
-struct ModeScratch {
-  void* p = nullptr;
-  explicit ModeScratch(size_t bytes) { check(cudaMalloc(&p, bytes) == cudaSuccess ? 0 : BRI17_ERR_CUDA, "cudaMalloc"); }
-  ~ModeScratch() { cudaFree(p); }
-  ModeScratch(const ModeScratch&) = delete;
-  ModeScratch& operator=(const ModeScratch&) = delete;
-};
 }  // namespace detail
 
 /** A rectangular periodic grid (include/bri17/bri17.hpp:34-159). */
@@ -141,46 +132,43 @@ class Hooke {
     return s.str();
   }
 
-  /** Hooke::modal_strain_displacement (:212-236): B has DIM entries. */
+  /** Hooke::modal_strain_displacement (:212-236): B has DIM entries.  One
+   *  kernel on the GPU per call (page-locked staging kept by the handle, no
+   *  allocation per call); batches amortise the launch. */
   void modal_strain_displacement(int const* k, std::complex<T>* B) const {
-    detail::ModeScratch m(16 + sizeof(std::complex<double>) * DIM);
     std::complex<double> out[DIM];
-    run_mode(m, k, [&](const int* kd, void* o) {
-      detail::check(bri17_modal_strain_displacement_batch(op_, kd, 1, o, nullptr),
-                    "bri17_modal_strain_displacement_batch");
-    }, out, DIM);
+    detail::check(bri17_modal_strain_displacement_host(op_, k, 1, out),
+                  "bri17_modal_strain_displacement_host");
     for (int i = 0; i < DIM; i++) B[i] = std::complex<T>(out[i]);
   }
 
   /** Hooke::modal_stiffness (:247-292): K has DIM*DIM entries (row-major). */
   void modal_stiffness(int const* k, std::complex<T>* K) const {
-    detail::ModeScratch m(16 + sizeof(std::complex<double>) * DIM * DIM);
     std::complex<double> out[DIM * DIM];
-    run_mode(m, k, [&](const int* kd, void* o) {
-      detail::check(bri17_modal_stiffness_batch(op_, kd, 1, o, nullptr),
-                    "bri17_modal_stiffness_batch");
-    }, out, DIM * DIM);
+    detail::check(bri17_modal_stiffness_host(op_, k, 1, out), "bri17_modal_stiffness_host");
     for (int i = 0; i < DIM * DIM; i++) K[i] = std::complex<T>(out[i]);
   }
 
   /** Hooke::modal_eigenstress_to_opposite_strain (:308-355). */
   void modal_eigenstress_to_opposite_strain(int const* k, std::complex<T> const* tau,
                                             std::complex<T>* eta) const {
-    detail::ModeScratch m(16 + 2 * sizeof(std::complex<double>) * sym);
-    int* kd = static_cast<int*>(m.p);
-    auto* td = reinterpret_cast<std::complex<double>*>(static_cast<char*>(m.p) + 16);
-    auto* ed = td + sym;
     std::complex<double> t[sym], e[sym];
     for (int i = 0; i < sym; i++) t[i] = std::complex<double>(tau[i]);
-    detail::check(cudaMemcpy(kd, k, sizeof(int) * DIM, cudaMemcpyHostToDevice) == cudaSuccess
-                      ? 0 : BRI17_ERR_CUDA, "cudaMemcpy");
-    detail::check(cudaMemcpy(td, t, sizeof(t), cudaMemcpyHostToDevice) == cudaSuccess
-                      ? 0 : BRI17_ERR_CUDA, "cudaMemcpy");
-    detail::check(bri17_modal_eigenstress_to_opposite_strain_batch(op_, kd, 1, td, ed, nullptr),
-                  "bri17_modal_eigenstress_to_opposite_strain_batch");
-    detail::check(cudaMemcpy(e, ed, sizeof(e), cudaMemcpyDeviceToHost) == cudaSuccess
-                      ? 0 : BRI17_ERR_CUDA, "cudaMemcpy");
+    detail::check(bri17_modal_eigenstress_to_opposite_strain_host(op_, k, 1, t, e),
+                  "bri17_modal_eigenstress_to_opposite_strain_host");
     for (int i = 0; i < sym; i++) eta[i] = std::complex<T>(e[i]);
+  }
+
+  /** Batched per-mode functions on host buffers (n modes; k is n x DIM,
+   *  outputs n x DIM*DIM / n x DIM complex, in double as the reference's
+   *  per-mode arithmetic runs in double). */
+  void modal_stiffness_batch(int const* k, int64_t n, std::complex<double>* K) const {
+    detail::check(bri17_modal_stiffness_host(op_, k, n, K), "bri17_modal_stiffness_host");
+  }
+  void modal_strain_displacement_batch(int const* k, int64_t n,
+                                       std::complex<double>* B) const {
+    detail::check(bri17_modal_strain_displacement_host(op_, k, n, B),
+                  "bri17_modal_strain_displacement_host");
   }
 
   // -- whole-field methods on device buffers (SoA, row-major nodes) ------
@@ -241,18 +229,6 @@ class Hooke {
     detail::check(bri17_op_create(DIM, shape, L, mu, nu, prec, &op_), "bri17_op_create");
   }
 
-  template <typename F>
-  void run_mode(detail::ModeScratch& m, int const* k, F&& fn, std::complex<double>* out,
-                int count) const {
-    int* kd = static_cast<int*>(m.p);
-    void* od = static_cast<char*>(m.p) + 16;
-    detail::check(cudaMemcpy(kd, k, sizeof(int) * DIM, cudaMemcpyHostToDevice) == cudaSuccess
-                      ? 0 : BRI17_ERR_CUDA, "cudaMemcpy");
-    fn(kd, od);
-    detail::check(cudaMemcpy(out, od, sizeof(std::complex<double>) * count,
-                             cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : BRI17_ERR_CUDA,
-                  "cudaMemcpy");
-  }
 };
 
 template <typename T, int DIM>

@@ -58,7 +58,10 @@ typedef enum bri17_status {
   BRI17_ERR_NO_DEVICE = 7,        /* no CUDA device visible */
   BRI17_ERR_BUSY = 8,             /* server full / request slot taken */
   BRI17_ERR_NOT_FOUND = 9,        /* unknown request id */
-  BRI17_ERR_CANCELLED = 10        /* request cancelled before it finished */
+  BRI17_ERR_CANCELLED = 10,       /* request cancelled before it finished */
+  BRI17_ERR_TIMEOUT = 11,         /* a bounded device wait ran out: results of
+                                     the work it belonged to are invalid */
+  BRI17_ERR_STAGNATED = 12        /* CG residual stopped decreasing above tol */
 } bri17_status;
 
 typedef enum bri17_precision {
@@ -160,6 +163,35 @@ int bri17_op_set_float_pair(bri17_op* op, int enable);
 int bri17_wait_timeouts(int* count);
 
 /*
+ * Failure of a bounded device wait, reported per handle (no reference
+ * counterpart).  The kernels that stage tiles by tensor copies (the FP32
+ * and float-pair axis-0 passes) wait for those copies at most one second;
+ * a wait that runs out, or a tile whose shared-memory window is misplaced,
+ * leaves that tile untransformed -- the output of that call is invalid --
+ * and sets the handle's status.  Stream-ordered calls return before their
+ * kernels run, so the failure reaches the caller as BRI17_ERR_TIMEOUT from:
+ *   - bri17_op_sync_status, which synchronises `stream` first;
+ *   - the synchronous entry points (bri17_apply_stiffness_host,
+ *     bri17_cg_solve) for their own work;
+ *   - the next field entry point called on the handle (apply_stiffness,
+ *     apply_stiffness_host, apply_strain, eigenstress_rhs,
+ *     eigenstress_to_opposite_strain, cg_solve), which then enqueues
+ *     nothing.
+ * Each failure is reported once; the handle stays usable.
+ */
+int bri17_op_sync_status(bri17_op* op, void* stream);
+
+/*
+ * Diagnostics (no reference counterpart): the limit, in nanoseconds of GPU
+ * global time, of the first wait on tile copies in the tensor-copy kernels
+ * on the current device; 0 makes every such wait give up at once (for
+ * testing the failure path).  Default 1e9 (one second).  A CTA whose wait
+ * gives up still waits, with the default limit, for its own copies to land
+ * before it leaves.
+ */
+int bri17_set_wait_limit_ns(uint64_t ns);
+
+/*
  * Batched Hooke::modal_stiffness (include/bri17/bri17.hpp:247-292; exported
  * to Python as Hooke*f64.modal_stiffness_matrix, python/pybri17.cpp:82-87).
  * k_dev: n x dim int32 multi-indices; K_dev: n x dim x dim complex (row-major
@@ -190,6 +222,26 @@ int bri17_modal_eigenstress_to_opposite_strain_batch(const bri17_op* op,
                                                      const void* tau_dev,
                                                      void* eta_dev,
                                                      void* stream);
+
+/*
+ * The three per-mode functions on host buffers, for code written against
+ * the reference's per-mode calls (include/bri17/bri17.hpp:212-355, called
+ * mode by mode from python/demo.py:34-40 and tests/test_bri17.cpp:63-91):
+ * k (n x dim int32), tau, K, B and eta are host memory in the layouts of
+ * the _batch functions above, with the same values (K bit for bit).  Each
+ * call copies its inputs into page-locked staging that the handle keeps
+ * (mapped into the device), runs one kernel on a private stream of the
+ * handle, waits for it and copies the result out: no device allocation
+ * after the first call of a size, and the caller's streams are not
+ * touched.  Synchronous; calls on one handle may come from several threads
+ * (they are serialised).  A call costs a kernel launch plus a
+ * synchronisation -- microseconds -- so batches of many modes amortise it.
+ */
+int bri17_modal_stiffness_host(const bri17_op* op, const int* k, int64_t n, void* K);
+int bri17_modal_strain_displacement_host(const bri17_op* op, const int* k, int64_t n,
+                                         void* B);
+int bri17_modal_eigenstress_to_opposite_strain_host(const bri17_op* op, const int* k,
+                                                    int64_t n, const void* tau, void* eta);
 
 /*
  * f = K u: the periodic stiffness operator, computed as
@@ -376,6 +428,18 @@ int bri17_server_step(bri17_server* srv, int* active);
  * reference counterpart. */
 int bri17_server_poll(bri17_server* srv, bri17_request_result* out, int cap,
                       int* count);
+
+/*
+ * Fault injection (diagnostics; no reference counterpart): the next bucket
+ * creation of this server fails at the allocation of its work buffer
+ * number `at` (0-based; the buffers allocated before it are released) as
+ * cudaMalloc does when device memory runs out; -1 cancels.  A request that
+ * cannot get a bucket -- injected or real out-of-memory, or a grid the
+ * operator rejects -- finishes alone with that status
+ * (BRI17_ERR_OUT_OF_MEMORY, ...); requests already in flight are not
+ * affected.
+ */
+int bri17_server_inject_alloc_failure(bri17_server* srv, int at);
 
 /* Cancel a queued or running request (its result reports CANCELLED).  No
  * reference counterpart. */

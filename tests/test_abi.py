@@ -66,6 +66,16 @@ def test_host_grid_api_matches_reference_fixture(golden_modal):
     assert g.get_node_at(2, 3, 4) == 59 and g.get_node_at(0, 1, 0) == 5
 
 
+def test_pybri17_importable_under_the_reference_name():
+    """``import pybri17`` (python/pybri17.cpp:98) finds the rebinding."""
+    import pybri17
+
+    from bri17_gb300 import pybri17 as inner
+    assert pybri17.Hooke3f64 is inner.Hooke3f64
+    assert pybri17.CartesianGrid2f64 is inner.CartesianGrid2f64
+    assert pybri17.__version__ == "0.1" and pybri17.__author__ == "S. Brisard"
+
+
 def test_pybri17_surface_and_contiguity_checks():
     from bri17_gb300 import pybri17
     assert pybri17.__author__ == "S. Brisard" and pybri17.__version__ == "0.1"

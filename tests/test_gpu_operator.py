@@ -215,6 +215,55 @@ def test_pybri17_per_mode_methods(golden_modal):
         h.modal_stiffness_matrix(c["k"][0], np.zeros((3, 3), np.complex128))
 
 
+@pytest.mark.parametrize("case", [0, 1])
+def test_per_mode_host_entry_points_match_device_batches(golden_modal, case):
+    """bri17_modal_*_host (host buffers, staging kept by the handle) give the
+    device batch entry points' values -- K and B bit for bit -- on batches of
+    one and of many modes, through the top-level ``pybri17`` name too."""
+    import ctypes
+    import time
+
+    import pybri17
+    from bri17_gb300 import _lib
+    c = golden_modal[case]
+    dim = len(c["shape"])
+    grid = (pybri17.CartesianGrid2f64 if dim == 2 else pybri17.CartesianGrid3f64)(
+        tuple(c["shape"]), tuple(c["L"]))
+    h = (pybri17.Hooke2f64 if dim == 2 else pybri17.Hooke3f64)(c["mu"], c["nu"], grid)
+    L = _lib.load()
+    k = np.ascontiguousarray(c["k"], dtype=np.intc)
+    n = k.shape[0]
+    K = np.empty((n, dim * dim), np.complex128)
+    B = np.empty((n, dim), np.complex128)
+    vp = ctypes.c_void_p
+    assert L.bri17_modal_stiffness_host(h.handle, vp(k.ctypes.data), n, vp(K.ctypes.data)) == 0
+    assert L.bri17_modal_strain_displacement_host(h.handle, vp(k.ctypes.data), n,
+                                                  vp(B.ctypes.data)) == 0
+    assert np.array_equal(K, h.modal_stiffness_batch(k).cpu().numpy().reshape(n, -1))
+    assert np.array_equal(B, h.modal_strain_displacement_batch(k).cpu().numpy())
+    inr = np.all((k >= 0) & (k < np.array(c["shape"])), axis=1)  # the fixture's in-range k
+    assert np.array_equal(K[inr], c["K"].reshape(n, -1)[inr])
+    sym = 3 if dim == 2 else 6
+    rng = np.random.default_rng(12)
+    tau = rng.standard_normal((n, sym)) + 1j * rng.standard_normal((n, sym))
+    eta = np.empty_like(tau)
+    assert L.bri17_modal_eigenstress_to_opposite_strain_host(
+        h.handle, vp(k.ctypes.data), n, vp(tau.ctypes.data), vp(eta.ctypes.data)) == 0
+    eta_dev = h.modal_eigenstress_to_opposite_strain_batch(k, tau).cpu().numpy()
+    assert np.array_equal(eta, eta_dev)
+    # One mode at a time through the reference's per-mode surface.
+    Ki = np.zeros(dim * dim, np.complex128)
+    etai = np.zeros(sym, np.complex128)
+    t0 = time.perf_counter()
+    for i in range(n):
+        h.modal_stiffness_matrix(k[i], Ki)
+        assert np.array_equal(Ki, K[i])
+    per_call_us = (time.perf_counter() - t0) / n * 1e6
+    h.modal_eigenstress_to_opposite_strain(k[3], np.ascontiguousarray(tau[3]), etai)
+    assert np.array_equal(etai, eta[3])
+    print(f"per-mode call through pybri17: {per_call_us:.1f} us")
+
+
 # Every form of the FP32 axis-0 stiffness pass against the oracle: register-
 # resident, shared-memory staged and TMA-staged (tensor copies of whole
 # tiles; 3D with an even shape[1]).  Shapes cover partial last tiles (P not a

@@ -54,6 +54,30 @@ def test_server_results_equal_solo_solves_and_oracle():
     srv.close()
 
 
+def test_served_results_equal_solo_solves_at_benchmark_sides():
+    """The same check at sides of the serving benchmark (32 and 48, cubic,
+    L = 1), several requests per bucket mixed with another geometry: each
+    served solution equals its solo mixed solve and the FP64 oracle within
+    the stated tolerance."""
+    from bri17_gb300.server import Server
+    rng = np.random.default_rng(13)
+    reqs = _requests(rng, 6, [32, 48])
+    srv = Server(memory_budget_bytes=4 << 30, slots_per_bucket=8)
+    ids = [srv.submit(*r, tol=TOL) for r in reqs]
+    results = {r["id"]: r for r in srv.run_until_idle()}
+    for rid, (shape, L, mu, nu, tau) in zip(ids, reqs):
+        res = results[rid]
+        assert res["status"] == 0 and res["rel_residual"] <= TOL, res
+        x_srv = srv.result(rid)
+        h, ho = pair(shape, L, mu, nu)
+        b = h.eigenstress_rhs(to_dev(tau))
+        x_solo, info = h.cg_solve(b, tol=TOL, mode="mixed")
+        x_ref = O.eigenstress_solve_half(ho, tau, workers=4)
+        assert rel_l2(x_srv, x_solo.cpu().numpy()) <= SOLUTION_TOL
+        assert rel_l2(x_srv, x_ref) <= SOLUTION_TOL
+    srv.close()
+
+
 def test_requests_are_admitted_while_others_run():
     """Two slots, five requests of one size: later requests enter slots freed
     by earlier ones while the other slot is still solving."""
