@@ -161,6 +161,17 @@ def traffic_from_profiles(kernel: str, workload: str):
         return None
 
 
+def traffic_source(kernel: str, workload: str):
+    """Where roofline.traffic comes from: the ncu capture recorded in
+    profiles/traffic.json (not measured by this run)."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        return "recorded in profiles/traffic.json: " + d[workload][kernel]["source"]
+    except Exception:
+        return None
+
+
 def pass_bytes(geom_dim, dof, cspec, comps, scalar):
     """Algorithmic bytes per launch of each pass: every pass reads its input
     array once and writes its output array once."""
@@ -466,6 +477,7 @@ def run_operator(args, precision="f64"):
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm_peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm_peak,
                 "traffic": traffic_from_profiles(dom, wl),
+                "traffic_source": traffic_source(dom, wl),
                 "algorithmic_bytes_per_launch": pb[dom], "avg_launch_ms": avg_ms}
         if dom == "axis0_fused":
             flops = fused_flops(shape, dim)
@@ -629,6 +641,25 @@ def cg_object(args, w, tau_fn, label, acc_tol=None):
                 "rel_residual": info["rel_residual"], "status": info["status_text"],
                 "error_vs_fp64_oracle": err_of(x)}
             del x
+    # The FP64-accurate plain solver on float pairs (operator in hi + lo
+    # floats on the FP32 pipe, FP64 vectors), reported beside the FP64-pipe
+    # solver; the speed-up of the mixed solver stays against the FP64 pipe.
+    try:
+        hooke.set_float_pair(True)
+    except Exception:
+        pass
+    else:
+        hooke.cg_solve(b, tol=1e-2, mode="plain", raise_on_failure=False)
+        for key, tol in tols:
+            sec, x, info = timed_solves(hooke, b, "plain", tol, 1)
+            out[key]["fp64_float_pair"] = {
+                "solves_per_s": 1.0 / sec, "seconds_per_solve": sec, "timed_solves": 1,
+                "iterations": info["iterations"], "rel_residual": info["rel_residual"],
+                "status": info["status_text"], "error_vs_fp64_oracle": err_of(x),
+                "method": "plain CG, operator in float pairs (48-bit significands on the "
+                          "FP32 pipe), FP64 vectors"}
+            del x
+        hooke.set_float_pair(False)
     clocks = sampler.stop()
     for key, tol in tols:
         o = out[key]

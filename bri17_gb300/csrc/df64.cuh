@@ -50,6 +50,8 @@ struct CplxOf<df64> {
   using type = df64c;
 };
 
+__device__ __forceinline__ df64 df_neg(df64 a) { return df64(-a.hi, -a.lo); }
+
 __device__ __forceinline__ df64 df_two_sum(float a, float b) {
   const float s = __fadd_rn(a, b);
   const float bb = __fadd_rn(s, -a);
@@ -79,6 +81,23 @@ __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
   return df_fast_two_sum(p, e);
+}
+
+// a * b + c * d with both products kept exact to the end (hi product plus
+// its FMA-computed error, and the cross terms) and a single error-free sum
+// and renormalisation: 19 float operations against 25 for two products and
+// a sum, with the same operand-relative bound as the sloppy sum,
+// |err| <= about 2^-46 (|a b| + |c d|).
+__device__ __forceinline__ df64 df_dot2(df64 a, df64 b, df64 c, df64 d) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float q = __fmul_rn(c.hi, d.hi);
+  float e = __fadd_rn(__fmaf_rn(a.hi, b.hi, -p), __fmaf_rn(c.hi, d.hi, -q));
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  e = __fmaf_rn(c.hi, d.lo, e);
+  e = __fmaf_rn(c.lo, d.hi, e);
+  const df64 s = df_two_sum(p, q);
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, e));
 }
 
 // a * b + c: df64, and the single-rounding FMA for float and double (these
@@ -204,6 +223,25 @@ __device__ __forceinline__ double to_io<df64>(df64 v) {
   if (e >= 0x7FF) return __longlong_as_double((long long)(sign | (0x7FFull << 52)));
   return __longlong_as_double(
       (long long)(sign | ((unsigned long long)e << 52) | ((unsigned long long)M & ((1ull << 52) - 1))));
+}
+
+// Complex products of float pairs: each part is one df_dot2 (the generic
+// forms would round each of the four products and the two sums).
+template <>
+__device__ __forceinline__ df64c cmul<df64>(df64c a, df64c b) {
+  df64c r;
+  r.x = df_dot2(a.x, b.x, df_neg(a.y), b.y);
+  r.y = df_dot2(a.x, b.y, a.y, b.x);
+  return r;
+}
+
+// a * conj(b)
+template <>
+__device__ __forceinline__ df64c cmulc<df64>(df64c a, df64c b) {
+  df64c r;
+  r.x = df_dot2(a.x, b.x, a.y, b.y);
+  r.y = df_dot2(a.y, b.x, df_neg(a.x), b.y);
+  return r;
 }
 
 }  // namespace bri17gb

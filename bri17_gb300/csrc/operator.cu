@@ -18,6 +18,10 @@
 #include "passes.cuh"
 #include "passes_p2.cuh"
 
+// The float-pair operator (defined with its C ABI below).
+static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
+                            cudaStream_t st);
+
 namespace bri17gb {
 
 static thread_local std::string g_last_error;
@@ -731,6 +735,11 @@ int apply_stiffness_async(bri17_op* op, const void* u, void* f,
                           cudaStream_t st) {
   int rc = ensure_spectrum(op, op->g.dim);
   if (rc != BRI17_OK) return rc;
+  // Float pairs on (bri17_op_set_float_pair): the CG solvers' FP64
+  // operator applications (the plain solver's, and the residuals of the
+  // reliable updates) run in float pairs too.
+  if (op->float_pair)
+    return ::run_stiffness_df(op, (const double*)u, (double*)f, op->fused_form_df, st);
   if (op->precision == BRI17_F64)
     return run_pipeline<double, kModeStiffness>(
         op, op->tab64, (const double*)u, (double*)f, 1, op->spec, nullptr, st);
@@ -1379,7 +1388,7 @@ static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
     PassScope ps(op, 0, st);
     ok = ct_rows_r2c<df64>(nl / 2, u, S, rows, g.H, tab.tw[dim - 1], none, st);
   }
-  if (ok) {
+  if (ok && dim == 3) {
     PassScope ps(op, 1, st);
     ok = ct_axis_c2c<df64, false>(g.n[1], S, g.H, (int64_t)dim * g.n[0], tab.tw[1], none, st);
   }
@@ -1388,14 +1397,17 @@ static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
     FusedParams<df64> fp = fused_params<df64>(op, tab, kModeStiffness);
     const int64_t bstride = (int64_t)dim * g.cspec;
     bool done = false;
-    if (form == 2)
+    if (form == 2 && dim == 3)
       done = ct_axis0_stiffness_tma_df(g.n[0], S, g.P, g.cspec, bstride, 1, fp, none, st);
-    if (!done)
+    if (!done && dim == 3)
       done = ct_axis0_stiffness_staged<df64, 3>(g.n[0], S, g.P, g.cspec, bstride, 1, fp, none,
+                                                st);
+    if (!done && dim == 2)
+      done = ct_axis0_stiffness_staged<df64, 2>(g.n[0], S, g.P, g.cspec, bstride, 1, fp, none,
                                                 st);
     ok = done;
   }
-  if (ok) {
+  if (ok && dim == 3) {
     PassScope ps(op, 3, st);
     ok = ct_axis_c2c<df64, true>(g.n[1], S, g.H, (int64_t)dim * g.n[0], tab.tw[1], none, st);
   }
@@ -1413,13 +1425,13 @@ static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
 }
 
 // Whether every pass of the grid has a compile-time float-pair instance:
-// 3D, power-of-two axes, shape[0] and shape[1] in 64..512, shape[2] in
-// 128..1024.
+// power-of-two axes, the strided ones (shape[0], and shape[1] in 3D) in
+// 64..512, the last one in 128..1024.
 static bool float_pair_supported(const Geometry& g) {
-  if (g.dim != 3) return false;
-  for (int i = 0; i < 2; i++)
+  for (int i = 0; i < g.dim - 1; i++)
     if (!is_pow2(g.n[i]) || g.n[i] < 64 || g.n[i] > 512) return false;
-  return is_pow2(g.n[2]) && g.n[2] >= 128 && g.n[2] <= 1024;
+  const int nl = g.n[g.dim - 1];
+  return is_pow2(nl) && nl >= 128 && nl <= 1024;
 }
 
 // Times the axis-0 forms of the float-pair operator on the handle's own
@@ -1475,13 +1487,14 @@ extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
     if (dc != BRI17_OK) return dc;
   }
   if (!enable) {
+    if (op->float_pair) op->material_epoch++;  // captured CG graphs hold the old form
     op->float_pair = false;
     return BRI17_OK;
   }
   if (op->precision != BRI17_F64) return invalid("float-pair arithmetic needs an FP64 handle");
   if (!float_pair_supported(op->g)) {
-    set_error("float-pair operator: 3D power-of-two grids, shape[0], shape[1] in 64..512, "
-              "shape[2] in 128..1024");
+    set_error("float-pair operator: power-of-two grids, the strided axes in 64..512, the "
+              "last axis in 128..1024");
     return BRI17_ERR_UNSUPPORTED_SIZE;
   }
   if (!op->table_df) {
@@ -1511,6 +1524,7 @@ extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
     if (rc != BRI17_OK) return rc;
     autotune_df_form(op);
   }
+  if (!op->float_pair) op->material_epoch++;  // captured CG graphs hold the old form
   op->float_pair = true;
   return BRI17_OK;
 }

@@ -7,6 +7,9 @@
 
 namespace bri17gb {
 
+template bool ct_axis0_stiffness_staged<df64, 2>(int, cplx<df64>*, int64_t, int64_t, int64_t,
+                                                 int, const FusedParams<df64>&, BatchMask,
+                                                 cudaStream_t);
 template bool ct_axis0_stiffness_staged<df64, 3>(int, cplx<df64>*, int64_t, int64_t, int64_t,
                                                  int, const FusedParams<df64>&, BatchMask,
                                                  cudaStream_t);
@@ -20,9 +23,12 @@ bool ct_axis0_stiffness_tma_df(int n0, cplx<df64>* X, int64_t P, int64_t cstride
 
 void ct_set_smem_attrs_df_axis0(size_t max_smem) {
 #define CASE(N)                                                                          \
-  if constexpr (ct_has<df64>(N))                                                         \
+  if constexpr (ct_has<df64>(N)) {                                                       \
+    cudaFuncSetAttribute(axis0_stiffness_staged<df64, 2, CtEng<N, 8>>,                   \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
     cudaFuncSetAttribute(axis0_stiffness_staged<df64, 3, CtEng<N, 8>>,                   \
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
+  }
   BRI17_CT_CASES(CASE)
 #undef CASE
   ct_set_smem_attrs_tma<df64, false>(max_smem);

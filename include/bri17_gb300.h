@@ -146,10 +146,12 @@ int bri17_op_set_fused_form(bri17_op* op, int form);
  * FP32 pipe, which GB300 runs at about 60x its FP64 rate) with FP64 fields
  * in memory.  Relative error against the FP64 operator is about 1e-14,
  * within the 1e-12 parity bound of the FP64 path.  Values keep their 48 bits
- * for magnitudes 1e-30..1e37.  3D power-of-two grids only: shape[0] and
- * shape[1] in 64..512, shape[2] in 128..1024 (else
- * BRI17_ERR_UNSUPPORTED_SIZE).  The other entry points of the handle
- * (strain, right-hand side, CG, per-mode batches) stay in FP64.  Off by
+ * for magnitudes 1e-30..1e37.  Power-of-two grids, 2D or 3D: the strided
+ * axes (shape[0], and shape[1] in 3D) in 64..512, the last axis in
+ * 128..1024 (else BRI17_ERR_UNSUPPORTED_SIZE).  The CG solvers' FP64
+ * operator applications on the handle (the plain solver's, and the FP64
+ * residuals of the mixed solver's reliable updates) run in float pairs too;
+ * strain, right-hand side and the per-mode batches stay in FP64.  Off by
  * default.
  */
 int bri17_op_set_float_pair(bri17_op* op, int enable);

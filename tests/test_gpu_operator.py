@@ -325,6 +325,8 @@ FLOAT_PAIR_SHAPES = [
     ((128, 128, 128), (1.0, 1.0, 1.0), 1.0, 0.25),
     ((64, 256, 256), (1.0, 2.0, 0.5), 0.8, 0.35),
     ((512, 64, 128), (1.0, 1.0, 0.125), 1.0, 0.35),
+    ((64, 128), (1.0, 1.0), 1.0, 0.3),
+    ((512, 1024), (1.0, 2.0), 0.7, 0.2),
 ]
 
 
@@ -334,7 +336,7 @@ def test_float_pair_operator_matches_oracle(shape, L, mu, nu):
     from bri17_gb300 import wait_timeouts
     h, ho = pair(shape, L, mu, nu)
     rng = np.random.default_rng(21)
-    u = mean_free_normal(rng, 3, shape)
+    u = mean_free_normal(rng, len(shape), shape)
     ud = to_dev(u)
     f64 = h.apply_stiffness(ud)
     h.set_float_pair(True)
@@ -365,7 +367,7 @@ def test_float_pair_host_buffers_and_rejected_grids():
     assert rel_l2(h.apply_stiffness_host(u), f_ref) <= TOL_F64
     up = torch.from_numpy(u).pin_memory()
     assert rel_l2(h.apply_stiffness_host(up).numpy(), f_ref) <= TOL_F64
-    for bad in ((48, 64, 128), (64, 64, 64), (32, 64, 128)):
+    for bad in ((48, 64, 128), (64, 64, 64), (32, 64, 128), (64, 64), (1024, 128)):
         hb, _ = pair(bad, (1.0, 1.0, 1.0), 1.0, 0.3)
         with pytest.raises(Bri17Error):
             hb.set_float_pair(True)

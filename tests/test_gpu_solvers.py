@@ -190,3 +190,27 @@ def test_cg_reaches_1e_8_error_against_the_oracle(mode):
     assert info["status"] == 0 and info["rel_residual"] <= 1e-11, info
     x_ref = O.eigenstress_solve_half(ho, tau, workers=4)
     assert rel_l2(x.cpu().numpy(), x_ref) <= 1e-8
+
+
+def test_cg_on_a_float_pair_handle():
+    """With float pairs on, the plain CG's operator applications (and the
+    mixed CG's FP64 residuals) run in float pairs: same accuracy against the
+    oracle as the FP64-pipe solvers, about the same iteration count."""
+    shape = (64, 64, 128)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3)
+    tau = np.random.default_rng(10).standard_normal((6,) + shape)
+    b = h.eigenstress_rhs(to_dev(tau))
+    x_ref = O.eigenstress_solve_half(ho, tau, workers=4)
+    res = {}
+    for fp in (False, True):
+        h.set_float_pair(fp)
+        for mode in ("plain", "mixed"):
+            x, info = h.cg_solve(b, tol=1e-11, mode=mode)
+            assert info["status"] == 0 and info["rel_residual"] <= 1e-11, (fp, mode, info)
+            res[(fp, mode)] = (rel_l2(x.cpu().numpy(), x_ref), info["iterations"])
+    h.set_float_pair(False)
+    for mode in ("plain", "mixed"):
+        e64, it64 = res[(False, mode)]
+        efp, itfp = res[(True, mode)]
+        assert efp <= max(2 * e64, 1e-9), (mode, efp, e64)
+        assert itfp <= 1.1 * it64 + 8, (mode, itfp, it64)
