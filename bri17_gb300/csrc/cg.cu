@@ -740,10 +740,20 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
         status = BRI17_ERR_STAGNATED;
         break;
       }
+      // The search direction is kept (rescaled to the new units) while the
+      // recomputed residual is close to the recursive one; when it is much
+      // larger (the FP32 recursion has run below what the FP64 residual
+      // resolves), p no longer fits r and alpha = r.r / p.Kp would be wrong:
+      // CG restarts from p = r.
+      const bool restart = rr64 > 4.0 * h.rr * sig * sig;
       rmax2 = rr64;
       const double sig_new = sqrt(rr64);
       k_to_f32<<<grid1(n), 256, 0, s>>>(w->r32, w->r, 1.0 / sig_new, n);
-      k_scale_f32<<<grid1(n), 256, 0, s>>>(w->p32, (float)(sig / sig_new), n);
+      if (restart)
+        BRI17_CUDA_TRY(cudaMemcpyAsync(w->p32, w->r32, n * sizeof(float),
+                                       cudaMemcpyDeviceToDevice, s));
+      else
+        k_scale_f32<<<grid1(n), 256, 0, s>>>(w->p32, (float)(sig / sig_new), n);
       sig = sig_new;
       k_dot<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->r32, n, w->st, w->partials);
       k_reliable_resume<<<1, 1, 0, s>>>(w->st, tol * tol * bb / rr64);

@@ -250,7 +250,13 @@ def test_per_mode_host_entry_points_match_device_batches(golden_modal, case):
     assert L.bri17_modal_eigenstress_to_opposite_strain_host(
         h.handle, vp(k.ctypes.data), n, vp(tau.ctypes.data), vp(eta.ctypes.data)) == 0
     eta_dev = h.modal_eigenstress_to_opposite_strain_batch(k, tau).cpu().numpy()
-    assert np.array_equal(eta, eta_dev)
+    # Same kernel, same inputs: identical, including the NaN a k that wraps
+    # to 0 without being 0 produces (K(k) = 0 there).
+    assert np.array_equal(eta, eta_dev, equal_nan=True)
+    ho = O.Hooke(c["mu"], c["nu"], O.Grid(c["shape"], c["L"]))
+    ref = np.array([ho.modal_eigenstress_to_opposite_strain(kk, t)
+                    for kk, t in zip(k[inr], tau[inr])])
+    assert np.abs(eta[inr] - ref).max() <= 1e-13 * np.abs(ref).max()
     # One mode at a time through the reference's per-mode surface.
     Ki = np.zeros(dim * dim, np.complex128)
     etai = np.zeros(sym, np.complex128)
@@ -259,8 +265,9 @@ def test_per_mode_host_entry_points_match_device_batches(golden_modal, case):
         h.modal_stiffness_matrix(k[i], Ki)
         assert np.array_equal(Ki, K[i])
     per_call_us = (time.perf_counter() - t0) / n * 1e6
-    h.modal_eigenstress_to_opposite_strain(k[3], np.ascontiguousarray(tau[3]), etai)
-    assert np.array_equal(etai, eta[3])
+    i3 = int(np.argwhere(inr)[3][0])
+    h.modal_eigenstress_to_opposite_strain(k[i3], np.ascontiguousarray(tau[i3]), etai)
+    assert np.array_equal(etai, eta[i3])
     print(f"per-mode call through pybri17: {per_call_us:.1f} us")
 
 
