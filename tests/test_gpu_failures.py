@@ -45,7 +45,10 @@ def zero_wait_limit():
     try:
         yield zero
     finally:
+        import torch
+        torch.cuda.synchronize()
         set_wait_limit_ns(DEFAULT_LIMIT_NS)
+        wait_timeouts()  # the counts this test made are not left for later tests
 
 
 def _tma_handle():

@@ -375,7 +375,7 @@ def test_float_pair_host_buffers_and_rejected_grids():
     up = torch.from_numpy(u).pin_memory()
     assert rel_l2(h.apply_stiffness_host(up).numpy(), f_ref) <= TOL_F64
     for bad in ((48, 64, 128), (64, 64, 64), (32, 64, 128), (64, 64), (1024, 128)):
-        hb, _ = pair(bad, (1.0, 1.0, 1.0), 1.0, 0.3)
+        hb, _ = pair(bad, (1.0,) * len(bad), 1.0, 0.3)
         with pytest.raises(Bri17Error):
             hb.set_float_pair(True)
     h32, _ = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3, precision="f32")
