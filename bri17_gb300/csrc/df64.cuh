@@ -100,6 +100,25 @@ __device__ __forceinline__ df64 df_dot2(df64 a, df64 b, df64 c, df64 d) {
   return df_fast_two_sum(s.hi, __fadd_rn(s.lo, e));
 }
 
+// a * b + c * d + e * f the same way: three exact products, two error-free
+// sums, one renormalisation (31 float operations against 43).
+__device__ __forceinline__ df64 df_dot3(df64 a, df64 b, df64 c, df64 d, df64 e, df64 f) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float q = __fmul_rn(c.hi, d.hi);
+  const float r = __fmul_rn(e.hi, f.hi);
+  float err = __fadd_rn(__fadd_rn(__fmaf_rn(a.hi, b.hi, -p), __fmaf_rn(c.hi, d.hi, -q)),
+                        __fmaf_rn(e.hi, f.hi, -r));
+  err = __fmaf_rn(a.hi, b.lo, err);
+  err = __fmaf_rn(a.lo, b.hi, err);
+  err = __fmaf_rn(c.hi, d.lo, err);
+  err = __fmaf_rn(c.lo, d.hi, err);
+  err = __fmaf_rn(e.hi, f.lo, err);
+  err = __fmaf_rn(e.lo, f.hi, err);
+  const df64 s1 = df_two_sum(p, q);
+  const df64 s2 = df_two_sum(s1.hi, r);
+  return df_fast_two_sum(s2.hi, __fadd_rn(__fadd_rn(s1.lo, s2.lo), err));
+}
+
 // a * b + c: df64, and the single-rounding FMA for float and double (these
 // overloads keep namespace-scope calls of fma(...) on the built-in FMA).
 __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) { return a * b + c; }
@@ -241,6 +260,40 @@ __device__ __forceinline__ df64c cmulc<df64>(df64c a, df64c b) {
   df64c r;
   r.x = df_dot2(a.x, b.x, a.y, b.y);
   r.y = df_dot2(a.y, b.x, df_neg(a.x), b.y);
+  return r;
+}
+
+// Sums inside a butterfly (fft.cuh badd / bsub / bnorm): the hi parts by
+// TwoSum, the lo parts added to its error term, without the final
+// renormalisation (8 float operations instead of 11); bnorm renormalises a
+// butterfly's outputs.  A sum of such pairs stays within the sloppy sum's
+// operand-relative bound to first order.
+__device__ __forceinline__ df64 df_add_nr(df64 a, df64 b) {
+  const df64 s = df_two_sum(a.hi, b.hi);
+  return df64(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+template <>
+__device__ __forceinline__ df64c badd<df64>(df64c a, df64c b) {
+  df64c r;
+  r.x = df_add_nr(a.x, b.x);
+  r.y = df_add_nr(a.y, b.y);
+  return r;
+}
+
+template <>
+__device__ __forceinline__ df64c bsub<df64>(df64c a, df64c b) {
+  df64c r;
+  r.x = df_add_nr(a.x, df_neg(b.x));
+  r.y = df_add_nr(a.y, df_neg(b.y));
+  return r;
+}
+
+template <>
+__device__ __forceinline__ df64c bnorm<df64>(df64c a) {
+  df64c r;
+  r.x = df_fast_two_sum(a.x.hi, a.x.lo);
+  r.y = df_fast_two_sum(a.y.hi, a.y.lo);
   return r;
 }
 

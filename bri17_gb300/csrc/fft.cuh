@@ -110,16 +110,42 @@ __device__ __forceinline__ void dft3(cplx<T>* v) {
   v[2] = csub<T>(t2, t3);
 }
 
-template <typename T, bool INV>
+// Sums inside a butterfly: cadd / csub, except that float pairs (df64.cuh)
+// leave out the renormalisation of each sum; bnorm restores it on values
+// that leave the butterfly.  For float and double all three are the plain
+// operations.
+template <typename T>
+__device__ __forceinline__ cplx<T> badd(cplx<T> a, cplx<T> b) {
+  return cadd<T>(a, b);
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> bsub(cplx<T> a, cplx<T> b) {
+  return csub<T>(a, b);
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> bnorm(cplx<T> a) {
+  return a;
+}
+
+// NORM = false leaves the outputs unnormalised (for a caller that goes on
+// summing them, as dft8 does).
+template <typename T, bool INV, bool NORM = true>
 __device__ __forceinline__ void dft4(cplx<T>* v) {
-  cplx<T> t0 = cadd<T>(v[0], v[2]);
-  cplx<T> t1 = csub<T>(v[0], v[2]);
-  cplx<T> t2 = cadd<T>(v[1], v[3]);
-  cplx<T> t3 = rot<T, INV>(csub<T>(v[1], v[3]));
-  v[0] = cadd<T>(t0, t2);
-  v[2] = csub<T>(t0, t2);
-  v[1] = cadd<T>(t1, t3);
-  v[3] = csub<T>(t1, t3);
+  cplx<T> t0 = badd<T>(v[0], v[2]);
+  cplx<T> t1 = bsub<T>(v[0], v[2]);
+  cplx<T> t2 = badd<T>(v[1], v[3]);
+  cplx<T> t3 = rot<T, INV>(bsub<T>(v[1], v[3]));
+  if constexpr (NORM) {
+    v[0] = bnorm<T>(badd<T>(t0, t2));
+    v[2] = bnorm<T>(bsub<T>(t0, t2));
+    v[1] = bnorm<T>(badd<T>(t1, t3));
+    v[3] = bnorm<T>(bsub<T>(t1, t3));
+  } else {
+    v[0] = badd<T>(t0, t2);
+    v[2] = bsub<T>(t0, t2);
+    v[1] = badd<T>(t1, t3);
+    v[3] = bsub<T>(t1, t3);
+  }
 }
 
 template <typename T, bool INV>
@@ -151,8 +177,8 @@ __device__ __forceinline__ void dft8(cplx<T>* v) {
   const T r = T(0.7071067811865475244008443621048490392848);
   cplx<T> e[4] = {v[0], v[2], v[4], v[6]};
   cplx<T> o[4] = {v[1], v[3], v[5], v[7]};
-  dft4<T, INV>(e);
-  dft4<T, INV>(o);
+  dft4<T, INV, false>(e);
+  dft4<T, INV, false>(o);
   // o[k] *= W8^k
   cplx<T> o1 = INV ? mk<T>(r * (o[1].x - o[1].y), r * (o[1].x + o[1].y))
                    : mk<T>(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x));

@@ -829,12 +829,12 @@ int cg_fused_iteration_async(bri17_op* op, const CgFusedBufs& B, cudaStream_t st
     PassScope ps(op, 0, st);
     ok = ct_rows_r2c_cg(m, cg, S, rows, g.H, tab.tw[2], mask, st);
   }
-  if (cudaError_t e = cudaPeekAtLastError()) return cuda_fail(e, "fused CG: rows_r2c_cg");
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: rows_r2c_cg");
   if (ok) {
     PassScope ps(op, 1, st);
     launch_axis1<float, false>(g, S, 3 * g.n[0], tab, mask, st);
   }
-  if (cudaError_t e = cudaPeekAtLastError()) return cuda_fail(e, "fused CG: axis-1 forward");
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: axis-1 forward");
   FusedParams<float> fp = fused_params<float>(op, tab, kModeStiffness);
   fp.dot.st = B.st;
   fp.dot.partials = B.part_dot;
@@ -848,12 +848,12 @@ int cg_fused_iteration_async(bri17_op* op, const CgFusedBufs& B, cudaStream_t st
     ok = ct_axis0_cg_dot_f32(g.n[0], env_form >= 0 ? env_form : op->fused_form, S, g.P, g.cspec,
                              fp, mask, st, &nctas);
   }
-  if (cudaError_t e = cudaPeekAtLastError()) return cuda_fail(e, "fused CG: axis-0 with p.Kp");
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: axis-0 with p.Kp");
   if (ok) {
     PassScope ps(op, 3, st);
     launch_axis1<float, true>(g, S, 3 * g.n[0], tab, mask, st);
   }
-  if (cudaError_t e = cudaPeekAtLastError()) return cuda_fail(e, "fused CG: axis-1 inverse");
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: axis-1 inverse");
   if (ok) {
     int64_t dot_bound = 0;
     cg_fused_ctas(op, &dot_bound, &cg.red.nparts);
@@ -863,7 +863,7 @@ int cg_fused_iteration_async(bri17_op* op, const CgFusedBufs& B, cudaStream_t st
     PassScope ps(op, 4, st);
     ok = ct_rows_c2r_cg(m, S, cg, rows, g.H, tab.tw[2], mask, st);
   }
-  if (cudaError_t e = cudaPeekAtLastError()) return cuda_fail(e, "fused CG: rows_c2r_cg");
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: rows_c2r_cg");
   if (!ok) {
     set_error("fused CG iteration: no compiled instance for this grid");
     return BRI17_ERR_UNSUPPORTED_SIZE;

@@ -12,20 +12,26 @@ bool ct_axis0_stiffness_tma_f32(int n0, bool keep, cplx<float>* X, int64_t P, in
   return ct_axis0_stiffness_tma<float>(n0, keep, X, P, cstride, bstride, batch, fp, mask, st);
 }
 
+// Raises a kernel's dynamic shared-memory limit to what the SM allows next
+// to its static shared memory (kernels with a block reduction declare some:
+// asking for the full max_smem would be refused and leave the 48 KB default).
+template <typename K>
+static void set_dyn_smem(K kernel, size_t max_smem) {
+  cudaFuncAttributes a;
+  if (cudaFuncGetAttributes(&a, kernel) != cudaSuccess) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(max_smem - a.sharedSizeBytes));
+}
+
 void ct_set_smem_attrs_tma_f32(size_t max_smem) {
   ct_set_smem_attrs_tma<float>(max_smem);
 #define CASE(N)                                                                          \
   if constexpr (N >= 16)                                                                 \
-    cudaFuncSetAttribute(axis0_stiffness_tma<float, 3, CtEng<N, 8>, false, true>,       \
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,                    \
-                         (int)std::min(max_smem, tma_smem_bytes<float, N>()));          \
-  cudaFuncSetAttribute(axis0_stiffness_staged<float, 3, CtEng<N, 8>, true>,             \
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);      \
+    set_dyn_smem(axis0_stiffness_tma<float, 3, CtEng<N, 8>, false, true>, max_smem);     \
+  set_dyn_smem(axis0_stiffness_staged<float, 3, CtEng<N, 8>, true>, max_smem);           \
   if constexpr (N <= 512) {                                                              \
-    cudaFuncSetAttribute(rows_r2c_cg<CtEng<N, 8>>,                                       \
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
-    cudaFuncSetAttribute(rows_c2r_cg<CtEng<N, 8>>,                                       \
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
+    set_dyn_smem(rows_r2c_cg<CtEng<N, 8>>, max_smem);                                    \
+    set_dyn_smem(rows_c2r_cg<CtEng<N, 8>>, max_smem);                                    \
   }
   BRI17_CT_CASES(CASE)
 #undef CASE

@@ -402,15 +402,30 @@ __device__ __forceinline__ void stiffness_lf(T phi0, T chi0, T psi0, const LineF
     const T K02 = sp0 * f.cp;
     const T K12 = (s * chi0) * f.pp;
     const cplx<T> u0 = u[0], u1 = u[1], u2 = u[2];
-    u[0] = mk<T>(K00 * u0.x + K01 * u1.x + K02 * u2.x, K00 * u0.y + K01 * u1.y + K02 * u2.y);
-    u[1] = mk<T>(K01 * u0.x + K11 * u1.x + K12 * u2.x, K01 * u0.y + K11 * u1.y + K12 * u2.y);
-    u[2] = mk<T>(K02 * u0.x + K12 * u1.x + K22 * u2.x, K02 * u0.y + K12 * u1.y + K22 * u2.y);
+    if constexpr (std::is_same<T, df64>::value) {
+      // Float pairs: each entry one fused three-term sum (df_dot3).
+      u[0] = mk<T>(df_dot3(K00, u0.x, K01, u1.x, K02, u2.x),
+                   df_dot3(K00, u0.y, K01, u1.y, K02, u2.y));
+      u[1] = mk<T>(df_dot3(K01, u0.x, K11, u1.x, K12, u2.x),
+                   df_dot3(K01, u0.y, K11, u1.y, K12, u2.y));
+      u[2] = mk<T>(df_dot3(K02, u0.x, K12, u1.x, K22, u2.x),
+                   df_dot3(K02, u0.y, K12, u1.y, K22, u2.y));
+    } else {
+      u[0] = mk<T>(K00 * u0.x + K01 * u1.x + K02 * u2.x, K00 * u0.y + K01 * u1.y + K02 * u2.y);
+      u[1] = mk<T>(K01 * u0.x + K11 * u1.x + K12 * u2.x, K01 * u0.y + K11 * u1.y + K12 * u2.y);
+      u[2] = mk<T>(K02 * u0.x + K12 * u1.x + K22 * u2.x, K02 * u0.y + K12 * u1.y + K22 * u2.y);
+    }
   } else {
     const T Kd = mu * (H00 + H11);
     const T K00 = s * H00 + Kd, K11 = s * H11 + Kd;
     const cplx<T> u0 = u[0], u1 = u[1];
-    u[0] = mk<T>(K00 * u0.x + K01 * u1.x, K00 * u0.y + K01 * u1.y);
-    u[1] = mk<T>(K01 * u0.x + K11 * u1.x, K01 * u0.y + K11 * u1.y);
+    if constexpr (std::is_same<T, df64>::value) {
+      u[0] = mk<T>(df_dot2(K00, u0.x, K01, u1.x), df_dot2(K00, u0.y, K01, u1.y));
+      u[1] = mk<T>(df_dot2(K01, u0.x, K11, u1.x), df_dot2(K01, u0.y, K11, u1.y));
+    } else {
+      u[0] = mk<T>(K00 * u0.x + K01 * u1.x, K00 * u0.y + K01 * u1.y);
+      u[1] = mk<T>(K01 * u0.x + K11 * u1.x, K01 * u0.y + K11 * u1.y);
+    }
   }
 }
 
