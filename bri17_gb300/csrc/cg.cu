@@ -11,7 +11,6 @@
 // block), and a chunk of iterations is replayed as one CUDA graph between
 // host checks of the residual.
 #include <math.h>
-#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
@@ -198,7 +197,6 @@ __global__ void __launch_bounds__(kRedThreads)
   if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) &&
       threadIdx.x == 0) {
     st->rr = tot;
-    st->beta = 0.0;  // the fused iteration forms p = r + beta p: p = r first
     st->thresh = rel_tol2 * st->aux;
     st->iters = 0;
     st->pause = 0;
@@ -241,15 +239,6 @@ struct CgWork {
   unsigned epoch64;
   unsigned epoch32;
   bool plain_ready;
-  // Fused FP32 iteration (cg_fused_iteration_async): its reduction
-  // partials and tickets, and its graph.
-  double* part_dot;
-  double* part_rr;
-  unsigned int* tickets;  // [0] p.Kp, [1] r.r
-  int64_t fused_dot_cap;
-  int64_t fused_rr_cap;
-  cudaGraphExec_t graph32f;
-  unsigned epoch32f;
 };
 
 static void cg_free(void* p) {
@@ -258,10 +247,6 @@ static void cg_free(void* p) {
   if (w->stream) cudaStreamSynchronize(w->stream);
   if (w->graph64) cudaGraphExecDestroy(w->graph64);
   if (w->graph32) cudaGraphExecDestroy(w->graph32);
-  if (w->graph32f) cudaGraphExecDestroy(w->graph32f);
-  cudaFree(w->part_dot);
-  cudaFree(w->part_rr);
-  cudaFree(w->tickets);
   cudaFree(w->x);
   cudaFree(w->r);
   cudaFree(w->p);
@@ -362,80 +347,6 @@ static int get_graph(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
   *epoch = opk->material_epoch;
-  return BRI17_OK;
-}
-
-// The fused FP32 iteration (operator.cu): buffers and a graph of kChunk
-// iterations plus the state's copy to the pinned mirror.
-// BRI17_CG_FUSED=0 keeps the unfused iteration (for measurements).
-static bool use_fused(const bri17_op* op32) {
-  static const bool off = [] {
-    const char* e = getenv("BRI17_CG_FUSED");
-    return e && strcmp(e, "0") == 0;
-  }();
-  return !off && cg_fused_supported(op32);
-}
-
-static int get_graph_fused(bri17_op* op32, CgWork* w) {
-  if (w->graph32f && w->epoch32f == op32->material_epoch) return BRI17_OK;
-  if (w->graph32f) {
-    cudaGraphExecDestroy(w->graph32f);
-    w->graph32f = nullptr;
-  }
-  int64_t dot = 0, rr = 0;
-  cg_fused_ctas(op32, &dot, &rr);
-  if (dot > w->fused_dot_cap || rr > w->fused_rr_cap || !w->tickets) {
-    cudaFree(w->part_dot);
-    cudaFree(w->part_rr);
-    w->part_dot = w->part_rr = nullptr;
-    w->fused_dot_cap = w->fused_rr_cap = 0;
-    BRI17_CUDA_TRY(cudaMalloc(&w->part_dot, dot * sizeof(double)));
-    BRI17_CUDA_TRY(cudaMalloc(&w->part_rr, rr * sizeof(double)));
-    w->fused_dot_cap = dot;
-    w->fused_rr_cap = rr;
-    if (!w->tickets) BRI17_CUDA_TRY(cudaMalloc(&w->tickets, 2 * sizeof(unsigned int)));
-  }
-  CgFusedBufs b;
-  b.d = w->d32;
-  b.r = w->r32;
-  b.p = w->p32;
-  b.st = w->st;
-  b.part_dot = w->part_dot;
-  b.ctr_dot = w->tickets;
-  b.part_rr = w->part_rr;
-  b.ctr_rr = w->tickets + 1;
-  // One iteration launched directly on a stopped state (every pass skips
-  // its work) before the capture: each kernel of the iteration is then
-  // loaded, and every launch path has run once, outside the capture.
-  {
-    CgState* scratch = nullptr;
-    BRI17_CUDA_TRY(cudaMalloc(&scratch, sizeof(CgState)));
-    BRI17_CUDA_TRY(cudaMemsetAsync(scratch, 0, sizeof(CgState), w->stream));
-    CgFusedBufs dry = b;
-    dry.st = scratch;
-    const int drc = cg_fused_iteration_async(op32, dry, w->stream);
-    const cudaError_t se = cudaStreamSynchronize(w->stream);
-    cudaFree(scratch);
-    if (drc != BRI17_OK) return drc;
-    if (se != cudaSuccess) return cuda_fail(se, "fused CG iteration (dry run)");
-  }
-  cudaGraph_t graph;
-  BRI17_CUDA_TRY(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = BRI17_OK;
-  for (int it = 0; it < kChunk && rc == BRI17_OK; it++)
-    rc = cg_fused_iteration_async(op32, b, w->stream);
-  if (rc == BRI17_OK) {
-    const cudaError_t ce = cudaMemcpyAsync(w->st_host, w->st, sizeof(CgState),
-                                           cudaMemcpyDeviceToHost, w->stream);
-    if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaMemcpyAsync(state)");
-  }
-  cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
-  if (rc != BRI17_OK) return rc;
-  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-  e = cudaGraphInstantiate(&w->graph32f, graph, 0);
-  cudaGraphDestroy(graph);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
-  w->epoch32f = op32->material_epoch;
   return BRI17_OK;
 }
 
@@ -781,17 +692,8 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
     k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
     k_start<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->p32, n, w->st, w->partials,
                                              tol * tol / rr64);
-    const bool fused = use_fused(op32);
-    if (fused) {
-      rc = get_graph_fused(op32, w);
-      if (rc != BRI17_OK) return rc;
-      BRI17_CUDA_TRY(cudaMemsetAsync(w->tickets, 0, 2 * sizeof(unsigned int), s));
-    } else {
-      rc = get_graph<float>(op32, w, w->d32, w->r32, w->p32, w->q32, &w->graph32,
-                            &w->epoch32);
-      if (rc != BRI17_OK) return rc;
-    }
-    cudaGraphExec_t chunk = fused ? w->graph32f : w->graph32;
+    rc = get_graph<float>(op32, w, w->d32, w->r32, w->p32, w->q32, &w->graph32, &w->epoch32);
+    if (rc != BRI17_OK) return rc;
     rc = read_state(w);
     if (rc != BRI17_OK) return rc;
     double rmax2 = rr64;  // squared norm at the last reliable update
@@ -800,7 +702,7 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
     int total = 0;
     int breakdowns = 0;  // consecutive FP32 breakdowns (p.Kp <= 0 or NaN)
     while (true) {
-      BRI17_CUDA_TRY(cudaGraphLaunch(chunk, s));
+      BRI17_CUDA_TRY(cudaGraphLaunch(w->graph32, s));
       BRI17_CUDA_TRY(cudaStreamSynchronize(s));
       const CgState h = *w->st_host;
       total = h.iters;
@@ -876,8 +778,6 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
       sig = sig_new;
       k_dot<float><<<rb, kRedThreads, 0, s>>>(w->r32, w->r32, n, w->st, w->partials);
       k_reliable_resume<<<1, 1, 0, s>>>(w->st, tol * tol * bb / rr64);
-      // A reduction cut short (a run-out wait) leaves a ticket behind.
-      if (fused) BRI17_CUDA_TRY(cudaMemsetAsync(w->tickets, 0, 2 * sizeof(unsigned int), s));
       rc = read_state(w);
       if (rc != BRI17_OK) return rc;
       if (!w->st_host->active) {

@@ -57,8 +57,6 @@ struct bri17_op {
 
 namespace bri17gb {
 
-struct CgState;  // cgstate.cuh
-
 constexpr int kHostEvents = 64;
 
 // Scalar byte size of a handle's fields.
@@ -94,26 +92,5 @@ int apply_stiffness_batched_async(bri17_op* op, int batch, const void* u,
                                   int flag_stride = 0);
 int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
                                   void* b, void* spec, cudaStream_t stream);
-
-// The fused CG iteration on an FP32 handle (3D, power-of-two axes with
-// compile-time row passes; cg_fused_supported): one operator application
-// whose first pass forms p = r + beta p as it reads it, whose axis-0 pass
-// sums p.Kp by Parseval and sets alpha, and whose last pass applies
-// d += alpha p, r -= alpha Kp and sums r.r (setting beta, rr, the iteration
-// count and the stop flag) -- five kernels, no vector kernels, and K p never
-// stored.  Every pass skips its work while st->active is 0.
-struct CgFusedBufs {
-  float* d;
-  float* r;
-  float* p;
-  CgState* st;
-  double* part_dot;  // >= cg_fused_ctas(...) dot partials
-  unsigned int* ctr_dot;
-  double* part_rr;   // >= cg_fused_ctas(...) r.r partials
-  unsigned int* ctr_rr;
-};
-bool cg_fused_supported(const bri17_op* op);
-void cg_fused_ctas(const bri17_op* op, int64_t* dot_ctas, int64_t* rr_ctas);
-int cg_fused_iteration_async(bri17_op* op, const CgFusedBufs& b, cudaStream_t stream);
 
 }  // namespace bri17gb

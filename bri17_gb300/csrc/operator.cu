@@ -14,7 +14,6 @@
 
 #include <cudaTypedefs.h>
 
-#include "cgstate.cuh"
 #include "op.cuh"
 #include "passes.cuh"
 #include "passes_p2.cuh"
@@ -573,8 +572,6 @@ static FusedParams<T> fused_params(const bri17_op* op, const Tables<T>& tab,
   fp.mat = nullptr;
   fp.form = op->fused_form;
   fp.status = op->status_dev;
-  memset(&fp.dot, 0, sizeof(fp.dot));
-  fp.nlast = op->g.n[op->g.dim - 1];
   return fp;
 }
 
@@ -772,103 +769,6 @@ int eigenstress_rhs_batched_async(bri17_op* op, int batch, const void* tau,
                                           (double*)b, batch, spec, nullptr, st);
   return run_pipeline<float, kModeRhs>(op, op->tab32, (const float*)tau,
                                        (float*)b, batch, spec, nullptr, st);
-}
-
-// ---------------------------------------------------------------------------
-// The fused CG iteration (FP32, 3D).  Each row pass is one launch over all
-// three components (the planes of component c follow those of c - 1 in the
-// field and in the spectrum).  Launching the last-axis and axis-1 passes per
-// chunk of planes, so that a chunk's spectrum is still in L2 for the next
-// pass, measured slower: every launch carries several microseconds of fixed
-// cost.
-
-static BatchMask cg_mask(CgState* st) {
-  BatchMask m;
-  m.flags = &st->active;
-  m.stride = 0;
-  m.unit = (int64_t)1 << 62;  // one entry: every CTA reads flags[0]
-  return m;
-}
-
-bool cg_fused_supported(const bri17_op* op) {
-  const Geometry& g = op->g;
-  if (op->precision != BRI17_F32 || g.dim != 3 || g.n[2] % 2 != 0) return false;
-  if (!g.use_p8_row || !g.use_p8[0] || !g.use_p8[1]) return false;
-  return g.p8_row.n >= 8 && g.p8_row.n <= 512 && g.n[0] >= 8 && g.n[0] <= 1024;
-}
-
-static int64_t cg_rows(const bri17_op* op) { return 3 * op->g.size / op->g.n[2]; }
-
-void cg_fused_ctas(const bri17_op* op, int64_t* dot_ctas, int64_t* rr_ctas) {
-  // The row passes' geometry depends only on whether a mask is present.
-  static const int any_flag = 1;
-  BatchMask mask;
-  mask.flags = &any_flag;
-  mask.stride = 0;
-  mask.unit = (int64_t)1 << 62;
-  *rr_ctas = ct_rows_ctas(op->g.p8_row.n, cg_rows(op), mask);
-  *dot_ctas = op->g.P;  // at least one line per CTA in every axis-0 form
-}
-
-int cg_fused_iteration_async(bri17_op* op, const CgFusedBufs& B, cudaStream_t st) {
-  const Geometry& g = op->g;
-  const Tables<float>& tab = op->tab32;
-  BatchMask mask = cg_mask(B.st);
-  const int m = g.p8_row.n;
-  const int64_t rows = cg_rows(op);
-  cplx<float>* S = reinterpret_cast<cplx<float>*>(op->spec);
-  set_smem_attrs<float>();
-  CgRows<float> cg;
-  cg.r = B.r;
-  cg.p = B.p;
-  cg.d = B.d;
-  memset(&cg.red, 0, sizeof(cg.red));
-  cg.red.st = B.st;
-  bool ok;
-  {
-    PassScope ps(op, 0, st);
-    ok = ct_rows_r2c_cg(m, cg, S, rows, g.H, tab.tw[2], mask, st);
-  }
-  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: rows_r2c_cg");
-  if (ok) {
-    PassScope ps(op, 1, st);
-    launch_axis1<float, false>(g, S, 3 * g.n[0], tab, mask, st);
-  }
-  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: axis-1 forward");
-  FusedParams<float> fp = fused_params<float>(op, tab, kModeStiffness);
-  fp.dot.st = B.st;
-  fp.dot.partials = B.part_dot;
-  fp.dot.counter = B.ctr_dot;
-  fp.dot.part_base = 0;
-  fp.dot.nparts = 0;  // the launch's own grid
-  const int env_form = env_fused_form();
-  int64_t nctas = 0;
-  if (ok) {
-    PassScope ps(op, 2, st);
-    ok = ct_axis0_cg_dot_f32(g.n[0], env_form >= 0 ? env_form : op->fused_form, S, g.P, g.cspec,
-                             fp, mask, st, &nctas);
-  }
-  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: axis-0 with p.Kp");
-  if (ok) {
-    PassScope ps(op, 3, st);
-    launch_axis1<float, true>(g, S, 3 * g.n[0], tab, mask, st);
-  }
-  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: axis-1 inverse");
-  if (ok) {
-    int64_t dot_bound = 0;
-    cg_fused_ctas(op, &dot_bound, &cg.red.nparts);
-    cg.red.partials = B.part_rr;
-    cg.red.counter = B.ctr_rr;
-    cg.red.part_base = 0;
-    PassScope ps(op, 4, st);
-    ok = ct_rows_c2r_cg(m, S, cg, rows, g.H, tab.tw[2], mask, st);
-  }
-  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e, "fused CG: rows_c2r_cg");
-  if (!ok) {
-    set_error("fused CG iteration: no compiled instance for this grid");
-    return BRI17_ERR_UNSUPPORTED_SIZE;
-  }
-  return BRI17_OK;
 }
 
 // Times the forms of the FP32 axis-0 stiffness pass (registers, staged,

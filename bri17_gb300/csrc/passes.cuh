@@ -40,33 +40,6 @@ struct BatchMask {
   }
 };
 
-struct CgState;  // cgstate.cuh
-
-// A conjugate-gradient reduction carried by an operator pass (st == null:
-// none).  Each CTA of the pass writes one partial sum at
-// partials[part_base + blockIdx.x] and takes a ticket; the CTA that takes
-// ticket nparts - 1 sums the partials in a fixed order (deterministic) and
-// updates the CG state.
-struct CgReduce {
-  CgState* st;
-  double* partials;
-  unsigned int* counter;
-  int64_t part_base;
-  int64_t nparts;
-};
-
-// The CG vectors of the fused iteration (FP32): the first pass forms the
-// search direction p = r + beta p (beta from the state) as it reads it, the
-// last applies x += alpha p, r -= alpha K p and sums r.r, so K p never
-// reaches memory.
-template <typename T>
-struct CgRows {
-  T* r;
-  T* p;
-  T* d;
-  CgReduce red;
-};
-
 template <typename T>
 struct FusedParams {
   Tables<T> tab;
@@ -79,8 +52,6 @@ struct FusedParams {
   const T* mat;     // optional per-batch (s, mu) pairs, overriding s, mu
   int form;         // power-of-two axis-0 stiffness pass: 0 registers, 1 staged
   int* status;      // the handle's status words (mapped host memory) or null
-  CgReduce dot;     // CG: p . K p by Parseval over the half spectrum (or none)
-  int nlast;        // cells along the last axis (half-spectrum weights of dot)
 };
 
 // ---------------------------------------------------------------------------

@@ -6,7 +6,6 @@
 
 #include <type_traits>
 
-#include "cgstate.cuh"
 #include "df64.cuh"
 #include "fft8.cuh"
 #include "fft8_ct.cuh"
@@ -183,147 +182,6 @@ __global__ void __launch_bounds__(kP2Threads)
   for (int q = 0; q < Eng::E; q++) xc[t + TT * q] = mk<Io>(to_io<T>(v[q].x), to_io<T>(v[q].y));
 }
 
-// CG iteration, first pass (FP32, n = 2m): the search direction is formed
-// as it is read, p = r + beta p (beta from the CG state; rows of p written
-// back), then transformed as rows_r2c_p2 transforms its input.
-template <class Eng>
-__global__ void __launch_bounds__(kP2Threads)
-    rows_r2c_cg(CgRows<float> cg, cplx<float>* __restrict__ X, int64_t nrows, int H, Eng pm,
-                const cplx<float>* __restrict__ tw_g, int RB, int pitch, BatchMask mask) {
-  using T = float;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int m = pm.n(), n = 2 * m, TT = pm.T();
-  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* twh = tw + n;
-  cplx<T>* bufs = twh + m + 1;
-  const int64_t row0 = (int64_t)blockIdx.x * RB;
-  const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
-  const int64_t row = row0 + rb;
-  const bool valid = rb < RB && row < nrows;
-  pdl_launch_dependents();
-  pm.template load_tw<T>(tw, tw_g, n, 2);
-  for (int i = threadIdx.x; i <= m; i += blockDim.x) {
-    const cplx<T> w = tw_g[i];
-    twh[i] = mk<T>(T(0.5) * w.x, T(0.5) * w.y);
-  }
-  pdl_wait();
-  if (mask.skip(row0)) return;
-  const T beta = (T)cg.red.st->beta;
-  cplx<T> v[Eng::E];
-  float2* pc = reinterpret_cast<float2*>(cg.p) + row * m;
-  const float2* rc = reinterpret_cast<const float2*>(cg.r) + row * m;
-#pragma unroll
-  for (int q = 0; q < Eng::E; q++) {
-    if (valid) {
-      const float2 rv = rc[t + TT * q], pv = pc[t + TT * q];
-      const float2 pn = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
-      pc[t + TT * q] = pn;
-      v[q] = mk<T>(pn.x, pn.y);
-    } else {
-      v[q] = mk<T>(T(0), T(0));
-    }
-  }
-  __syncthreads();
-  cplx<T>* buf = bufs + rb * pitch;
-  pm.template run<T, false>(v, buf, t, tw, 2);
-#pragma unroll
-  for (int q = 0; q < Eng::E; q++) buf[pad16(t + TT * q)] = v[q];
-  __syncthreads();
-  if (!valid) return;
-  cplx<T>* out = X + row * H;
-#pragma unroll
-  for (int q = 0; q < Eng::E; q++) {
-    const int k = t + TT * q;
-    const cplx<T> zk = v[q];
-    const cplx<T> zm = buf[pad16((m - k) & (m - 1))];
-    const cplx<T> A = mk<T>(zk.x + zm.x, zk.y - zm.y);
-    const cplx<T> D = mk<T>(zk.y + zm.y, zm.x - zk.x);
-    const cplx<T> WD = cmul<T>(twh[k], D);
-    out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
-  }
-  if (t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
-}
-
-// CG iteration, last pass (FP32): the rows of q = K p come out of the
-// inverse transform in registers and are used at once -- x += alpha p,
-// r -= alpha q, with the partial sums of r.r -- instead of being stored.
-// The last CTA sets rr, beta = rr_new / rr and the iteration count, and
-// stops the CG (active = 0) when rr has met the threshold or is not finite.
-template <class Eng>
-__global__ void __launch_bounds__(kP2Threads)
-    rows_c2r_cg(const cplx<float>* __restrict__ X, CgRows<float> cg, int64_t nrows, int H,
-                Eng pm, const cplx<float>* __restrict__ tw_g, int RB, int pitch,
-                BatchMask mask) {
-  using T = float;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int m = pm.n(), n = 2 * m, TT = pm.T();
-  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* stw = tw + n;
-  cplx<T>* bufs = stw + (Eng::template stage<T>() ? m : 0);
-  const int64_t row0 = (int64_t)blockIdx.x * RB;
-  const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
-  const int64_t row = row0 + rb;
-  const bool valid = rb < RB && row < nrows;
-  pdl_launch_dependents();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
-  if constexpr (Eng::template stage<T>()) pm.template load_tw<T>(stw, tw_g, n, 2);
-  __syncthreads();
-  pdl_wait();
-  if (mask.skip(row0)) return;
-  const T alpha = (T)cg.red.st->alpha;
-  cplx<T> v[Eng::E];
-  const cplx<T>* in = X + row * H;
-#pragma unroll
-  for (int q = 0; q < Eng::E; q++) {
-    const int k = t + TT * q;
-    if (valid) {
-      const cplx<T> xk = in[k];
-      const cplx<T> xm = in[m - k];
-      const cplx<T> A = mk<T>(xk.x + xm.x, xk.y - xm.y);
-      const cplx<T> D = mk<T>(xk.x - xm.x, xk.y + xm.y);
-      const cplx<T> Bv = cmulc<T>(D, tw[k]);
-      v[q] = mk<T>(A.x - Bv.y, A.y + Bv.x);
-    } else {
-      v[q] = mk<T>(T(0), T(0));
-    }
-  }
-  pm.template run<T, true>(v, bufs + rb * pitch, t, Eng::template stage<T>() ? stw : tw, 2);
-  T acc = T(0);
-  if (valid) {
-    float2* rc = reinterpret_cast<float2*>(cg.r) + row * m;
-    float2* dc = reinterpret_cast<float2*>(cg.d) + row * m;
-    const float2* pc = reinterpret_cast<const float2*>(cg.p) + row * m;
-#pragma unroll
-    for (int q = 0; q < Eng::E; q++) {
-      const int i = t + TT * q;
-      const float2 pv = pc[i];
-      float2 rv = rc[i], dv = dc[i];
-      dv.x = fmaf(alpha, pv.x, dv.x);
-      dv.y = fmaf(alpha, pv.y, dv.y);
-      rv.x = fmaf(-alpha, v[q].x, rv.x);
-      rv.y = fmaf(-alpha, v[q].y, rv.y);
-      acc += rv.x * rv.x + rv.y * rv.y;
-      rc[i] = rv;
-      dc[i] = dv;
-    }
-  }
-  double tot;
-  if (last_block_total_at((double)acc, cg.red.partials, cg.red.counter, cg.red.part_base,
-                          cg.red.nparts, &tot) &&
-      threadIdx.x == 0) {
-    CgState* st = cg.red.st;
-    st->iters += 1;
-    if (!isfinite(tot)) {
-      st->flag = BRI17_ERR_BREAKDOWN;
-      st->active = 0;
-    } else {
-      st->beta = tot / st->rr;
-      st->rr = tot;
-      if (tot <= st->thresh) st->active = 0;
-    }
-  }
-}
-
 // Middle axis: complex [A][n][B], lines along n; TB consecutive inner
 // indices per CTA, consecutive threads on consecutive lines (coalesced).
 template <typename T, bool INV, class Eng>
@@ -429,45 +287,6 @@ __device__ __forceinline__ void stiffness_lf(T phi0, T chi0, T psi0, const LineF
   }
 }
 
-// CG through the axis-0 pass (FP32 forms with DOT): p . K p summed over the
-// modes by Parseval -- for real p and the real symmetric K(k) of any mode,
-// sum_x p(x) (K p)(x) = sum_k conj(p^(k)) . M(k) p^(k), with M(k) the
-// per-mode operator including the |h|/|N| normalisation, as computed here
-// -- so the real-space K p need not be read back.  Only the half spectrum
-// is stored: a line at k_last = 0, or at k_last = n_last / 2 for even
-// n_last, stands for itself, every other line also for its conjugate.
-__device__ __forceinline__ float half_weight(int64_t line, int H, int nlast) {
-  const int k = (int)(line % H);
-  return (k == 0 || 2 * k == nlast) ? 1.f : 2.f;
-}
-
-template <typename T, int DIM>
-__device__ __forceinline__ T mode_dot(const cplx<T>* a, const cplx<T>* b) {
-  T s = T(0);
-#pragma unroll
-  for (int c = 0; c < DIM; c++) s += a[c].x * b[c].x + a[c].y * b[c].y;
-  return s;
-}
-
-// The last CTA of the pass turns the partial sums into p.Kp and alpha =
-// r.r / p.Kp (breakdown when p.Kp is not positive and finite).  Every thread
-// of the CTA calls it.
-__device__ __forceinline__ void cg_dot_finish(double acc, const CgReduce& red) {
-  double tot;
-  const int64_t nparts = red.nparts ? red.nparts : (int64_t)gridDim.x;
-  if (last_block_total_at(acc, red.partials, red.counter, red.part_base, nparts, &tot) &&
-      threadIdx.x == 0) {
-    CgState* st = red.st;
-    st->pq = tot;
-    if (!(tot > 0.0) || !isfinite(tot)) {
-      st->flag = BRI17_ERR_BREAKDOWN;
-      st->active = 0;
-    } else {
-      st->alpha = st->rr / tot;
-    }
-  }
-}
-
 // Axis 0, fused stiffness: forward DFT of the DIM components along axis 0,
 // K(k) u(k) in registers, inverse DFT, in place (as axis0_fused with
 // kModeStiffness).
@@ -554,7 +373,7 @@ namespace bri17gb {
 // own positions (no barrier needed: a thread reads back only what it wrote),
 // K(k) u(k) runs from there, and the inverse transforms read it back.  Half
 // the registers of the register-resident form, so twice the warps per SM.
-template <typename T, int DIM, class Eng, bool DOT = false>
+template <typename T, int DIM, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
     axis0_stiffness_staged(cplx<T>* __restrict__ X, int64_t P, int64_t cstride,
                            int64_t bstride, int TB, int pitch, Eng p0, FusedParams<T> fp,
@@ -612,23 +431,17 @@ __global__ void __launch_bounds__(kP2Threads)
     psi2 = ldg_val(fp.tab.kpsi[2] + k2);
   }
   const LineFactors<T> lf = line_factors<T, DIM>(phi1, chi1, psi1, phi2, chi2, psi2);
-  T dacc = T(0);
 #pragma unroll 2
   for (int q = 0; q < Eng::E; q++) {
     const int k0 = t + p0.T() * q;
     const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
             psi0 = ldg_val(fp.tab.kpsi[0] + k0);
-    cplx<T> u[DIM], u_in[DIM];
+    cplx<T> u[DIM];
 #pragma unroll
-    for (int c = 0; c < DIM; c++) u[c] = u_in[c] = stash[((size_t)c * TB + tb) * spitch + k0];
+    for (int c = 0; c < DIM; c++) u[c] = stash[((size_t)c * TB + tb) * spitch + k0];
     stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
-    if constexpr (DOT) dacc += mode_dot<T, DIM>(u_in, u);
 #pragma unroll
     for (int c = 0; c < DIM; c++) stash[((size_t)c * TB + tb) * spitch + k0] = u[c];
-  }
-  if constexpr (DOT) {
-    static_assert(std::is_same<T, float>::value && DIM == 3, "CG dot: FP32, 3D");
-    cg_dot_finish(valid ? (double)(dacc * half_weight(b, fp.H, fp.nlast)) : 0.0, fp.dot);
   }
 #pragma unroll 1
   for (int c = 0; c < DIM; c++) {
@@ -663,7 +476,7 @@ static __device__ unsigned long long g_tma_wait_limit_ns = kWaitLimitNs;
 // registers at a time); true keeps all DIM components in registers from the
 // forward transforms through K(k) u(k) to the inverse ones (fewer
 // shared-memory round trips, more registers).
-template <typename T, int DIM, class Eng, bool KEEP, bool DOT = false>
+template <typename T, int DIM, class Eng, bool KEEP>
 __global__ void __launch_bounds__(256)
     axis0_stiffness_tma(const __grid_constant__ CUtensorMap map, int64_t P, int TB, int pitch,
                         Eng p0, FusedParams<T> fp, BatchMask mask) {
@@ -771,23 +584,17 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
     }
-    T dacc = T(0);
 #pragma unroll 2
     for (int q = 0; q < Eng::E; q++) {
       const int k0 = t + p0.T() * q;
       const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
               psi0 = ldg_val(fp.tab.kpsi[0] + k0);
-      cplx<T> u[DIM], u_in[DIM];
+      cplx<T> u[DIM];
 #pragma unroll
-      for (int c = 0; c < DIM; c++) u[c] = u_in[c] = tile[((size_t)c * n0 + k0) * TB + tb];
+      for (int c = 0; c < DIM; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
       stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
-      if constexpr (DOT) dacc += mode_dot<T, DIM>(u_in, u);
 #pragma unroll
       for (int c = 0; c < DIM; c++) tile[((size_t)c * n0 + k0) * TB + tb] = u[c];
-    }
-    if constexpr (DOT) {
-      static_assert(std::is_same<T, float>::value && !KEEP, "CG dot: FP32, staged compute");
-      cg_dot_finish(valid ? (double)(dacc * half_weight(b, fp.H, fp.nlast)) : 0.0, fp.dot);
     }
 #pragma unroll 1
     for (int c = 0; c < DIM; c++) {
@@ -836,19 +643,6 @@ bool ct_axis0_stiffness_tma_f32(int n0, bool keep, cplx<float>* X, int64_t P, in
                                 int64_t bstride, int batch, const FusedParams<float>& fp,
                                 BatchMask mask, cudaStream_t st);
 void ct_set_smem_attrs_tma_f32(size_t max_smem);
-// The fused CG iteration's passes (FP32, 3D, compile-time lengths; false
-// when the length has no instance): the row passes of rows_r2c_cg /
-// rows_c2r_cg, their CTA count per launch, and the axis-0 pass with the
-// p.Kp reduction (TMA-staged for forms 2 and 3 where its layout rules hold,
-// else shared-memory staged; *nctas receives the CTAs launched).
-int ct_rows_ctas(int m, int64_t nrows, const BatchMask& mask);
-bool ct_rows_r2c_cg(int m, CgRows<float> cg, cplx<float>* X, int64_t nrows, int H,
-                    const cplx<float>* tw, BatchMask mask, cudaStream_t st);
-bool ct_rows_c2r_cg(int m, const cplx<float>* X, CgRows<float> cg, int64_t nrows, int H,
-                    const cplx<float>* tw, BatchMask mask, cudaStream_t st);
-bool ct_axis0_cg_dot_f32(int n0, int form, cplx<float>* X, int64_t P, int64_t cstride,
-                         const FusedParams<float>& fp, BatchMask mask, cudaStream_t st,
-                         int64_t* nctas);
 // Float-pair instances (passes_ct_df.cu, passes_df_rows.cu, passes_df_c2c.cu):
 // the staged and TMA axis-0 forms, rows and axis-1 passes, lengths 64..512.
 bool ct_axis0_stiffness_tma_df(int n0, cplx<df64>* X, int64_t P, int64_t cstride,
