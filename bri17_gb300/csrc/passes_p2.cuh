@@ -574,6 +574,15 @@ __global__ void __launch_bounds__(256)
       for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[c][q];
     }
   } else {
+    // One component in registers at a time, the others parked in the tile.
+    // FP32 (KL): the last component's forward transform stays in registers
+    // through K(k) u(k) and is the first to be transformed back, which
+    // spares it four shared-memory passes (park, K read, K write, reload):
+    // 80 registers instead of 64, pass time 131 -> 129 us at 256^3 and
+    // 268 -> 260 us at 512x512x128.  Float pairs keep every component in
+    // the tile (their registers are the constraint: the same change made
+    // that pass slower, 80 -> 92 us at 128^3).
+    constexpr bool KL = std::is_same<T, float>::value;
     cplx<T> v[Eng::E];
 #pragma unroll 1
     for (int c = 0; c < DIM; c++) {
@@ -581,26 +590,48 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
       p0.template run<T, false>(v, buf, t, tw, 1);
+      if (!KL || c < DIM - 1) {
 #pragma unroll
-      for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
+        for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
+      }
     }
+    if constexpr (KL) {
+#pragma unroll
+      for (int q = 0; q < Eng::E; q++) {
+        const int k0 = t + p0.T() * q;
+        const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
+                psi0 = ldg_val(fp.tab.kpsi[0] + k0);
+        cplx<T> u[DIM];
+#pragma unroll
+        for (int c = 0; c < DIM - 1; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
+        u[DIM - 1] = v[q];
+        stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
+#pragma unroll
+        for (int c = 0; c < DIM - 1; c++) tile[((size_t)c * n0 + k0) * TB + tb] = u[c];
+        v[q] = u[DIM - 1];
+      }
+    } else {
 #pragma unroll 2
-    for (int q = 0; q < Eng::E; q++) {
-      const int k0 = t + p0.T() * q;
-      const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
-              psi0 = ldg_val(fp.tab.kpsi[0] + k0);
-      cplx<T> u[DIM];
+      for (int q = 0; q < Eng::E; q++) {
+        const int k0 = t + p0.T() * q;
+        const T phi0 = ldg_val(fp.tab.kphi[0] + k0), chi0 = ldg_val(fp.tab.kchi[0] + k0),
+                psi0 = ldg_val(fp.tab.kpsi[0] + k0);
+        cplx<T> u[DIM];
 #pragma unroll
-      for (int c = 0; c < DIM; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
-      stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
+        for (int c = 0; c < DIM; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
+        stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
 #pragma unroll
-      for (int c = 0; c < DIM; c++) tile[((size_t)c * n0 + k0) * TB + tb] = u[c];
+        for (int c = 0; c < DIM; c++) tile[((size_t)c * n0 + k0) * TB + tb] = u[c];
+      }
     }
 #pragma unroll 1
-    for (int c = 0; c < DIM; c++) {
+    for (int i = 0; i < DIM; i++) {
+      const int c = KL ? (i == 0 ? DIM - 1 : i - 1) : i;
       cplx<T>* tc = tile + (size_t)c * n0 * TB + tb;
+      if (!KL || i > 0) {
 #pragma unroll
-      for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
+        for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
+      }
       p0.template run<T, true>(v, buf, t, tw, 1);
 #pragma unroll
       for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
