@@ -465,12 +465,12 @@ static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
   if (g.use_p8[1]) {
     const Plan8& p = g.p8[1];
     if (ct_axis_c2c<T, INV>(p.n, X, g.H, nouter, tab.tw[1], mask, st)) return BRI17_OK;
-    const int TB = (int)std::min<int64_t>(kP2Threads / p.T, g.H);
+    const int TB = (int)std::min<int64_t>(kP2Threads / p.T, nouter * g.H);
     const int pitch = exchange_pitch(p.n, TB, (int)sizeof(cplx<T>), true);
     const size_t smem = (p.n + (size_t)TB * pitch) * sizeof(cplx<T>);
-    dim3 grid((unsigned)((g.H + TB - 1) / TB), (unsigned)nouter);
-    launch_pdl(axis_c2c_p2<T, INV, RtEng>, grid, p.T * TB, smem, st, X, g.H, TB, RtEng{p},
-               tab.tw[1], pitch, mask);
+    const int64_t nl = nouter * g.H;
+    launch_pdl(axis_c2c_p2<T, INV, RtEng>, (unsigned)((nl + TB - 1) / TB), p.T * TB, smem, st, X,
+               g.H, nl, TB, RtEng{p}, tab.tw[1], pitch, mask);
     return BRI17_OK;
   }
   const int n = g.n[1];

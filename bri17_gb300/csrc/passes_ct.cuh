@@ -122,23 +122,24 @@ bool ct_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw
       if (c2c_e16()) {                                                                 \
         constexpr int E16 = 16;                                                        \
         const int TT = N / E16;                                                        \
-        const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B)); \
+        const int TB =                                                                 \
+            (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, nouter * B)); \
         const int pitch = exchange_pitch(N, TB, (int)sizeof(cplx<T>), true, E16);      \
         const size_t smem = (N + (size_t)TB * pitch) * sizeof(cplx<T>);                \
-        dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);                    \
-        launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E16>>, grid, TT * TB, smem, st, X, B, TB, \
-                   CtEng<N, E16>{}, tw, pitch, mask);                                  \
+        const int64_t nl = nouter * B;                                                 \
+        launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E16>>, (unsigned)((nl + TB - 1) / TB),  \
+                   TT * TB, smem, st, X, B, nl, TB, CtEng<N, E16>{}, tw, pitch, mask); \
         return true;                                                                   \
       }                                                                                \
     }                                                                                  \
     constexpr int E = CtE<T, N>::value;                                                \
     const int TT = N / E;                                                              \
-    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, B));   \
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, nouter * B)); \
     const int pitch = exchange_pitch(N, TB, (int)sizeof(cplx<T>), true);               \
     const size_t smem = (N + (size_t)TB * pitch) * sizeof(cplx<T>);                    \
-    dim3 grid((unsigned)((B + TB - 1) / TB), (unsigned)nouter);                        \
-    launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E>>, grid, TT * TB, smem, st, X, B, TB, CtEng<N, E>{}, \
-                                                                  tw, pitch, mask);    \
+    const int64_t nl = nouter * B;                                                     \
+    launch_pdl(axis_c2c_p2<T, INV, CtEng<N, E>>, (unsigned)((nl + TB - 1) / TB), TT * TB, \
+               smem, st, X, B, nl, TB, CtEng<N, E>{}, tw, pitch, mask);                \
     return true;                                                                       \
     }                                                                                 \
   }

@@ -26,6 +26,7 @@ namespace bri17gb {
 // keep the cheaper natural copy.  stage<S>() tells which table run reads.
 struct RtEng {
   static constexpr int E = 8;
+  static constexpr int kTT = 0;  // threads per line: known at run time only
   template <typename S>
   static constexpr bool stage() {
     return false;
@@ -48,6 +49,7 @@ struct RtEng {
 template <int N, int EE = 8>
 struct CtEng {
   static constexpr int E = EE;
+  static constexpr int kTT = N / EE;
   template <typename S>
   static constexpr bool stage() {
     return !std::is_same<S, df64>::value;
@@ -75,10 +77,53 @@ struct CtEng {
 constexpr int kP2Threads = 256;
 constexpr int kP2FusedThreads = 128;
 
+// Resident CTAs per SM that the forward row pass asks the register
+// allocator for: FP32 fits 32 registers (eight 256-thread CTAs, the whole
+// SM; 40 registers and six CTAs measured 79 -> 86 us at 256^3), float pairs
+// 64 (four); FP64 is bound by the FP64 pipe and takes what the compiler
+// picks.  The inverse row pass keeps the compiler's choice (FP32: 40
+// registers; capped at 32 it spills and measured 84 -> 89 us at 256^3).
+template <typename T>
+struct RowCtas {
+  static constexpr int value = std::is_same<T, float>::value ? 8
+                               : std::is_same<T, df64>::value ? 4
+                                                              : 1;
+};
+
+// Warp shuffle of a complex value (float, double or float pair).
+template <typename T>
+__device__ __forceinline__ cplx<T> shfl_cplx(unsigned lanes, cplx<T> v, int src) {
+  if constexpr (std::is_same<T, df64>::value) {
+    cplx<T> r;
+    r.x = df64(__shfl_sync(lanes, v.x.hi, src), __shfl_sync(lanes, v.x.lo, src));
+    r.y = df64(__shfl_sync(lanes, v.y.hi, src), __shfl_sync(lanes, v.y.lo, src));
+    return r;
+  } else {
+    return mk<T>(__shfl_sync(lanes, v.x, src), __shfl_sync(lanes, v.y, src));
+  }
+}
+
+// The half-spectrum split of a row of m = TT E complex points held as
+// v[q] = Z[t + TT q] (TT threads per row, a power of two <= 32, so a row
+// lies in one warp) needs Z[(m - k) mod m] beside each Z[k]:
+// for t > 0 that is element E-1-q of the row's thread TT - t, for t = 0 its
+// own element (E - q) mod E.  mirror_lane gives the source lane of the
+// shuffle and warp_lanes the lanes present in the calling thread's warp
+// (the last warp of a small CTA may be partial; rows never straddle it).
+template <int TT>
+__device__ __forceinline__ int mirror_lane(int t) {
+  const int lane = threadIdx.x & 31;
+  return (lane & ~(TT - 1)) | ((TT - t) & (TT - 1));
+}
+__device__ __forceinline__ unsigned warp_lanes() {
+  const int present = (int)blockDim.x - (int)(threadIdx.x & ~31u);
+  return present >= 32 ? 0xffffffffu : ((1u << present) - 1u);
+}
+
 // Last axis, forward (n = 2m, m a power of two >= 8): rows of n reals ->
 // n/2+1 complex.  T = m/8 threads per row, RB rows per CTA.
 template <typename T, class Eng>
-__global__ void __launch_bounds__(kP2Threads)
+__global__ void __launch_bounds__(kP2Threads, RowCtas<T>::value)
     rows_r2c_p2(const typename IoOf<T>::type* __restrict__ x, cplx<T>* __restrict__ X,
                 int64_t nrows, int H, Eng pm, const cplx<T>* __restrict__ tw_g, int RB,
                 int pitch, BatchMask mask) {
@@ -114,10 +159,21 @@ __global__ void __launch_bounds__(kP2Threads)
   __syncthreads();
   cplx<T>* buf = bufs + rb * pitch;
   pm.template run<T, false>(v, buf, t, tw, 2);
+  // Z_{m-k}: from the row's mirror thread by warp shuffles when a row lies
+  // in one warp (every lane stays to the end: shuffles name whole rows),
+  // else through the exchange buffer.
+  constexpr bool kShfl = Eng::kTT > 0 && Eng::kTT <= 32;
+  unsigned lanes = 0;
+  int src = 0;
+  if constexpr (kShfl) {
+    lanes = warp_lanes();
+    src = mirror_lane<Eng::kTT>(t);
+  } else {
 #pragma unroll
-  for (int q = 0; q < Eng::E; q++) buf[pad16(t + TT * q)] = v[q];
-  __syncthreads();
-  if (!valid) return;
+    for (int q = 0; q < Eng::E; q++) buf[pad16(t + TT * q)] = v[q];
+    __syncthreads();
+    if (!valid) return;
+  }
   cplx<T>* out = X + row * H;
   // X_k = (A + W D) / 2 with A = Z_k + conj(Z_{m-k}), D = -i (Z_k -
   // conj(Z_{m-k})); the 1/2 lives in the twh table and one fused
@@ -126,13 +182,19 @@ __global__ void __launch_bounds__(kP2Threads)
   for (int q = 0; q < Eng::E; q++) {
     const int k = t + TT * q;
     const cplx<T> zk = v[q];
-    const cplx<T> zm = buf[pad16((m - k) & (m - 1))];
+    cplx<T> zm;
+    if constexpr (kShfl) {
+      const cplx<T> o = shfl_cplx<T>(lanes, v[Eng::E - 1 - q], src);
+      zm = t == 0 ? v[(Eng::E - q) % Eng::E] : o;
+    } else {
+      zm = buf[pad16((m - k) & (m - 1))];
+    }
     const cplx<T> A = mk<T>(zk.x + zm.x, zk.y - zm.y);
     const cplx<T> D = mk<T>(zk.y + zm.y, zm.x - zk.x);
     const cplx<T> WD = cmul<T>(twh[k], D);
-    out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
+    if (valid) out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
   }
-  if (t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
+  if (valid && t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
 }
 
 // Last axis, inverse: n/2+1 complex -> n reals (unnormalised).
@@ -161,18 +223,43 @@ __global__ void __launch_bounds__(kP2Threads)
   if (mask.skip(row0)) return;
   cplx<T> v[Eng::E];
   const cplx<T>* in = X + row * H;
+  constexpr bool kShfl = Eng::kTT > 0 && Eng::kTT <= 32;
+  if constexpr (kShfl) {
+    // Each thread loads its own X_k once; X_{m-k} comes from the row's
+    // mirror thread by warp shuffles (X_m, which no thread holds, is loaded
+    // by thread 0 of the row).
+    const cplx<T> zero = mk<T>(T(0), T(0));
+    cplx<T> w[Eng::E];
 #pragma unroll
-  for (int q = 0; q < Eng::E; q++) {
-    const int k = t + TT * q;
-    if (valid) {
-      const cplx<T> xk = in[k];
-      const cplx<T> xm = in[m - k];
+    for (int q = 0; q < Eng::E; q++) w[q] = valid ? in[t + TT * q] : zero;
+    const cplx<T> wm = (valid && t == 0) ? in[m] : zero;
+    const unsigned lanes = warp_lanes();
+    const int src = mirror_lane<Eng::kTT>(t);
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++) {
+      const int k = t + TT * q;
+      const cplx<T> o = shfl_cplx<T>(lanes, w[Eng::E - 1 - q], src);
+      const cplx<T> xk = w[q];
+      const cplx<T> xm = t != 0 ? o : (q == 0 ? wm : w[(Eng::E - q) % Eng::E]);
       const cplx<T> A = mk<T>(xk.x + xm.x, xk.y - xm.y);
       const cplx<T> D = mk<T>(xk.x - xm.x, xk.y + xm.y);
       const cplx<T> Bv = cmulc<T>(D, tw[k]);
       v[q] = mk<T>(A.x - Bv.y, A.y + Bv.x);
-    } else {
-      v[q] = mk<T>(T(0), T(0));
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++) {
+      const int k = t + TT * q;
+      if (valid) {
+        const cplx<T> xk = in[k];
+        const cplx<T> xm = in[m - k];
+        const cplx<T> A = mk<T>(xk.x + xm.x, xk.y - xm.y);
+        const cplx<T> D = mk<T>(xk.x - xm.x, xk.y + xm.y);
+        const cplx<T> Bv = cmulc<T>(D, tw[k]);
+        v[q] = mk<T>(A.x - Bv.y, A.y + Bv.x);
+      } else {
+        v[q] = mk<T>(T(0), T(0));
+      }
     }
   }
   pm.template run<T, true>(v, bufs + rb * pitch, t, Eng::template stage<T>() ? stw : tw, 2);
@@ -182,24 +269,32 @@ __global__ void __launch_bounds__(kP2Threads)
   for (int q = 0; q < Eng::E; q++) xc[t + TT * q] = mk<Io>(to_io<T>(v[q].x), to_io<T>(v[q].y));
 }
 
-// Middle axis: complex [A][n][B], lines along n; TB consecutive inner
-// indices per CTA, consecutive threads on consecutive lines (coalesced).
+// Middle axis: complex [A][n][B], lines along n.  The A * B lines are
+// numbered plane-major (line = a B + b) and dealt out TB consecutive lines
+// per CTA, consecutive threads on consecutive lines (coalesced; a CTA may
+// straddle two planes).  With B = n_last/2 + 1 odd, a grid over b alone
+// would leave one CTA per plane holding a single line (a fifth of the
+// CTAs at 128^3, a ninth at 256^3) running full transforms on zeros.
 template <typename T, bool INV, class Eng>
 __global__ void __launch_bounds__(kP2Threads)
-    axis_c2c_p2(cplx<T>* __restrict__ X, int64_t B, int TB, Eng p,
+    axis_c2c_p2(cplx<T>* __restrict__ X, int64_t B, int64_t nlines, int TB, Eng p,
                 const cplx<T>* __restrict__ tw_g, int pitch, BatchMask mask) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = p.n();
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* bufs = tw + n;
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
-  const int64_t b = (int64_t)blockIdx.x * TB + tb;
-  const bool valid = b < B;
-  cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b;
+  const int64_t line = (int64_t)blockIdx.x * TB + tb;
+  const int64_t a = line / B;
+  bool valid = line < nlines;
+  cplx<T>* base = X + a * n * B + (line - a * B);
   pdl_launch_dependents();
   p.template load_tw<T>(tw, tw_g, n, 1);
   pdl_wait();
-  if (mask.skip(blockIdx.y)) return;
+  if (mask.flags) {
+    valid = valid && !mask.skip(a);
+    if (!__syncthreads_or(valid)) return;
+  }
   cplx<T> v[Eng::E];
 #pragma unroll
   for (int q = 0; q < Eng::E; q++)
