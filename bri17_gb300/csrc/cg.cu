@@ -394,9 +394,11 @@ static void project_mean(bri17_op* op, CgWork* w, double* a) {
   k_sub_mean<<<grid2, 256, 0, w->stream>>>(a, size, w->st);
 }
 
-// r = b - K x (FP64) and aux = r.r.
-static int residual64(bri17_op* op, CgWork* w, const double* b) {
-  int rc = apply_stiffness_async(op, w->x, w->q, w->stream);
+// r = b - K x (FP64 accurate; the mixed solvers' in float pairs where
+// prepare_accurate_residual enabled them).
+static int residual64(bri17_op* op, CgWork* w, const double* b, bool mixed = false) {
+  int rc = mixed ? apply_accurate_async(op, w->x, w->q, w->stream)
+                 : apply_stiffness_async(op, w->x, w->q, w->stream);
   if (rc != BRI17_OK) return rc;
   k_residual<<<grid1(w->n), 256, 0, w->stream>>>(w->r, b, w->q, w->n);
   return BRI17_OK;
@@ -534,6 +536,8 @@ static int solve_mixed(bri17_op* op, const double* b, double* x, double tol,
   CgWork* w;
   int rc = ensure_work(op, true, &w);
   if (rc != BRI17_OK) return rc;
+  rc = prepare_accurate_residual(op);
+  if (rc != BRI17_OK) return rc;
   const int64_t n = w->n;
   cudaStream_t s = w->stream;
   const int rb = red_blocks(n);
@@ -561,7 +565,7 @@ static int solve_mixed(bri17_op* op, const double* b, double* x, double tol,
   const int max_outer = 40;
   for (int outer = 0; outer <= max_outer; outer++) {
     project_mean(op, w, w->x);
-    rc = residual64(op, w, b);
+    rc = residual64(op, w, b, true);
     if (rc != BRI17_OK) return rc;
     project_mean(op, w, w->r);
     k_dot<double><<<rb, kRedThreads, 0, s>>>(w->r, w->r, n, w->st, w->partials);
@@ -641,6 +645,8 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
   CgWork* w;
   int rc = ensure_work(op, true, &w);
   if (rc != BRI17_OK) return rc;
+  rc = prepare_accurate_residual(op);
+  if (rc != BRI17_OK) return rc;
   const int64_t n = w->n;
   cudaStream_t s = w->stream;
   const int rb = red_blocks(n);
@@ -665,7 +671,7 @@ static int solve_mixed_reliable(bri17_op* op, const double* b, double* x, double
   // r = b - K x (FP64), projected; FP32 copies; p = r32; d = 0.
   auto true_residual = [&](double* rr_out) -> int {
     project_mean(op, w, w->x);
-    int e = residual64(op, w, b);
+    int e = residual64(op, w, b, true);
     if (e != BRI17_OK) return e;
     project_mean(op, w, w->r);
     k_dot<double><<<rb, kRedThreads, 0, s>>>(w->r, w->r, n, w->st, w->partials);

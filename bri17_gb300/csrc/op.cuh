@@ -39,6 +39,9 @@ struct bri17_op {
   int fused_form_df;
   void* table_df;
   bri17gb::Tables<bri17gb::df64> tabdf;
+  // The mixed solvers' FP64 residuals (reliable updates) run in float pairs
+  // (set by prepare_accurate_residual).
+  bool residual_df;
   // Status words the handle's kernels set when a bounded device wait runs
   // out ([0]) or a tile is skipped ([1]): page-locked host memory mapped
   // into the device, read by the host without a copy.
@@ -80,6 +83,16 @@ int ensure_spectrum(bri17_op* op, int comps);
 // Enqueue f = K u on `stream` for a handle of either precision.
 int apply_stiffness_async(bri17_op* op, const void* u, void* f,
                           cudaStream_t stream);
+
+// FP64-accurate f = K u for the mixed solvers' reliable updates.
+// prepare_accurate_residual (called before a solve, outside any stream
+// capture) builds the float-pair tables when the grid has float-pair
+// instances, unless BRI17_MIXED_RESIDUAL=f64 (for measurements) or the
+// handle is already in float pairs; apply_accurate_async then runs the
+// float-pair operator (relative difference ~1e-14 from the FP64 operator, at
+// about four times its speed on GB300), else the handle's own operator.
+int prepare_accurate_residual(bri17_op* op);
+int apply_accurate_async(bri17_op* op, const double* u, double* f, cudaStream_t stream);
 
 // Batched forms used by the server: `batch` fields of one geometry,
 // contiguous (entry z at z * dim * size), with per-entry material

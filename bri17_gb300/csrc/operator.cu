@@ -659,6 +659,7 @@ static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
   cplx<T>* S = reinterpret_cast<cplx<T>*>(spec);
   const int64_t bstride = (int64_t)cmax * g.cspec;
   set_smem_attrs<T>();
+  PdlScope chain(pdl_for_entries((int64_t)batch * cmax * g.cspec));
   // Launch over entries [z0, z0 + nz): one launch when their data are
   // contiguous (c == cmax or a single entry), else one per entry.
   auto mask_at = [&](int z0, int64_t unit) {
@@ -1383,6 +1384,7 @@ static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
   none.unit = 1;
   const int nl = g.n[dim - 1];
   const int64_t rows = (int64_t)dim * (g.size / nl);
+  PdlScope chain(pdl_for_entries((int64_t)dim * g.cspec));
   bool ok;
   {
     PassScope ps(op, 0, st);
@@ -1480,6 +1482,8 @@ static void autotune_df_form(bri17_op* op) {
   cudaGetLastError();
 }
 
+static int ensure_float_pair_tables(bri17_op* op);
+
 extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
   if (!op) return invalid("null handle");
   {
@@ -1497,6 +1501,16 @@ extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
               "last axis in 128..1024");
     return BRI17_ERR_UNSUPPORTED_SIZE;
   }
+  const int rc = ensure_float_pair_tables(op);
+  if (rc != BRI17_OK) return rc;
+  if (!op->float_pair) op->material_epoch++;  // captured CG graphs hold the old form
+  op->float_pair = true;
+  return BRI17_OK;
+}
+
+// Float-pair tables, kernel attributes and axis-0 form of an FP64 handle
+// whose grid has float-pair instances (built once).
+static int ensure_float_pair_tables(bri17_op* op) {
   if (!op->table_df) {
     const Geometry& g = op->g;
     std::vector<HostTables> ht(g.dim);
@@ -1524,9 +1538,31 @@ extern "C" int bri17_op_set_float_pair(bri17_op* op, int enable) {
     if (rc != BRI17_OK) return rc;
     autotune_df_form(op);
   }
-  if (!op->float_pair) op->material_epoch++;  // captured CG graphs hold the old form
-  op->float_pair = true;
   return BRI17_OK;
+}
+
+int bri17gb::prepare_accurate_residual(bri17_op* op) {
+  static const bool f64_only = [] {
+    const char* e = getenv("BRI17_MIXED_RESIDUAL");
+    return e && strcmp(e, "f64") == 0;
+  }();
+  op->residual_df = false;
+  if (f64_only || op->float_pair || op->precision != BRI17_F64 ||
+      !float_pair_supported(op->g))
+    return BRI17_OK;
+  const int rc = ensure_float_pair_tables(op);
+  if (rc != BRI17_OK) return rc;
+  op->residual_df = true;
+  return BRI17_OK;
+}
+
+int bri17gb::apply_accurate_async(bri17_op* op, const double* u, double* f, cudaStream_t st) {
+  if (op->residual_df && !op->float_pair) {
+    const int rc = ensure_spectrum(op, op->g.dim);
+    if (rc != BRI17_OK) return rc;
+    return ::run_stiffness_df(op, u, f, op->fused_form_df, st);
+  }
+  return apply_stiffness_async(op, u, f, st);
 }
 
 extern "C" int bri17_apply_stiffness(bri17_op* op, const void* u, void* f,

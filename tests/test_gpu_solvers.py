@@ -193,9 +193,10 @@ def test_cg_reaches_1e_8_error_against_the_oracle(mode):
 
 
 def test_cg_on_a_float_pair_handle():
-    """With float pairs on, the plain CG's operator applications (and the
-    mixed CG's FP64 residuals) run in float pairs: same accuracy against the
-    oracle as the FP64-pipe solvers, about the same iteration count."""
+    """With float pairs on, the plain CG's operator applications run in
+    float pairs: same accuracy against the oracle as the FP64-pipe solver,
+    about the same iteration count.  (The mixed CG's FP64 residuals run in
+    float pairs on this grid either way.)"""
     shape = (64, 64, 128)
     h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3)
     tau = np.random.default_rng(10).standard_normal((6,) + shape)
