@@ -148,11 +148,11 @@ int bri17_op_set_fused_form(bri17_op* op, int form);
  * within the 1e-12 parity bound of the FP64 path.  Values keep their 48 bits
  * for magnitudes 1e-30..1e37.  Power-of-two grids, 2D or 3D: the strided
  * axes (shape[0], and shape[1] in 3D) in 64..512, the last axis in
- * 128..1024 (else BRI17_ERR_UNSUPPORTED_SIZE).  The CG solvers' FP64
- * operator applications on the handle (the plain solver's, and the FP64
- * residuals of the mixed solver's reliable updates) run in float pairs too;
- * strain, right-hand side and the per-mode batches stay in FP64.  Off by
- * default.
+ * 128..1024 (else BRI17_ERR_UNSUPPORTED_SIZE).  The plain CG solver's
+ * operator applications on the handle run in float pairs too (the mixed
+ * solvers' FP64 residuals use them on such grids either way: see
+ * bri17_cg_solve); strain, right-hand side and the per-mode batches stay in
+ * FP64.  Off by default.
  */
 int bri17_op_set_float_pair(bri17_op* op, int enable);
 
@@ -349,8 +349,13 @@ typedef struct bri17_cg_info {
  * translations, sphinx/theory.rst eq. (17) note).  b_dev and x_dev are FP64
  * (dim x size).  On entry x_dev is the initial guess (zero it for a cold
  * start).  BRI17_CG_MIXED needs an FP64 handle; it builds an FP32 twin
- * internally on first use.  Synchronises `stream` (the stopping test reads
- * the residual).
+ * internally on first use.  The mixed modes compute their FP64 residuals
+ * (r = b - K x) in float pairs (see bri17_op_set_float_pair; about 1e-14
+ * from the FP64 operator) whenever the grid has float-pair instances, with
+ * float pairs on the handle or not; BRI17_MIXED_RESIDUAL=f64 in the
+ * environment keeps them on the FP64 pipe.  The plain solver on an FP64
+ * handle stays on the FP64 pipe unless float pairs are on.  Synchronises
+ * `stream` (the stopping test reads the residual).
  */
 int bri17_cg_solve(bri17_op* op, const double* b_dev, double* x_dev,
                    double tol, int max_iterations, int mode,
