@@ -13,6 +13,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "op.cuh"
@@ -231,6 +233,7 @@ struct CgWork {
   float* p32;
   float* q32;
   double* partials;
+  double* pq_part;   // per-CTA partials of p.Kp from the FP32 stiffness pass
   CgState* st;
   CgState* st_host;  // pinned mirror
   cudaStream_t stream;
@@ -256,6 +259,7 @@ static void cg_free(void* p) {
   cudaFree(w->p32);
   cudaFree(w->q32);
   cudaFree(w->partials);
+  cudaFree(w->pq_part);
   cudaFree(w->st);
   cudaFreeHost(w->st_host);
   if (w->stream) cudaStreamDestroy(w->stream);
@@ -276,6 +280,7 @@ static int ensure_work(bri17_op* op, bool mixed, CgWork** out) {
     BRI17_CUDA_TRY(cudaMalloc(&w->r, n * sizeof(double)));
     BRI17_CUDA_TRY(cudaMalloc(&w->q, n * sizeof(double)));
     BRI17_CUDA_TRY(cudaMalloc(&w->partials, 6 * kRedMaxBlocks * sizeof(double)));
+    BRI17_CUDA_TRY(cudaMalloc(&w->pq_part, (size_t)std::max<int64_t>(op->g.P, 1) * sizeof(double)));
     BRI17_CUDA_TRY(cudaMalloc(&w->st, sizeof(CgState)));
     BRI17_CUDA_TRY(cudaMemset(w->st, 0, sizeof(CgState)));
     BRI17_CUDA_TRY(cudaMallocHost(&w->st_host, sizeof(CgState)));
@@ -316,10 +321,20 @@ static int enqueue_chunk(bri17_op* opk, CgWork* w, T* x, T* r, T* p, T* q,
                          cudaStream_t s) {
   const int64_t n = w->n;
   const int rb = red_blocks(n);
+  // FP32: p.Kp summed by Parseval in the stiffness pass where the handle's
+  // form allows (no separate pass over p and q).
+  bool fused = false;
+  if constexpr (std::is_same<T, float>::value) fused = cg_pq_fusable(opk) && w->pq_part;
   for (int it = 0; it < kChunk; it++) {
-    int rc = apply_stiffness_async(opk, p, q, s);
+    int rc;
+    if constexpr (std::is_same<T, float>::value) {
+      rc = fused ? apply_stiffness_cg_async(opk, p, q, w->st, w->pq_part, s)
+                 : apply_stiffness_async(opk, p, q, s);
+    } else {
+      rc = apply_stiffness_async(opk, p, q, s);
+    }
     if (rc != BRI17_OK) return rc;
-    k_dot_pq<T><<<rb, kRedThreads, 0, s>>>(p, q, n, w->st, w->partials);
+    if (!fused) k_dot_pq<T><<<rb, kRedThreads, 0, s>>>(p, q, n, w->st, w->partials);
     k_update<T><<<rb, kRedThreads, 0, s>>>(x, r, p, q, n, w->st, w->partials);
     k_pupdate<T><<<grid1(n), 256, 0, s>>>(p, r, n, w->st);
     k_apply_pause<<<1, 32, 0, s>>>(w->st, 1);

@@ -4,6 +4,10 @@
 #include "common.cuh"
 #include "df64.cuh"
 
+namespace bri17gb {
+struct CgState;
+}
+
 struct bri17_op {
   bri17gb::Geometry g;
   double L[3];
@@ -42,6 +46,10 @@ struct bri17_op {
   // The mixed solvers' FP64 residuals (reliable updates) run in float pairs
   // (set by prepare_accurate_residual).
   bool residual_df;
+  // Set around a CG iteration's operator application on an FP32 handle
+  // (apply_stiffness_cg_async): the axis-0 pass sums p.Kp into this state.
+  bri17gb::CgState* cg_st;
+  double* cg_part;
   // Status words the handle's kernels set when a bounded device wait runs
   // out ([0]) or a tile is skipped ([1]): page-locked host memory mapped
   // into the device, read by the host without a copy.
@@ -93,6 +101,14 @@ int apply_stiffness_async(bri17_op* op, const void* u, void* f,
 // about four times its speed on GB300), else the handle's own operator.
 int prepare_accurate_residual(bri17_op* op);
 int apply_accurate_async(bri17_op* op, const double* u, double* f, cudaStream_t stream);
+
+// CG iterations on FP32 handles: whether the handle's stiffness pass can
+// sum p.Kp by Parseval (3D power-of-two grid with an even last axis, the
+// TMA-staged axis-0 form), and the application that does so into st->pq and
+// st->alpha (one partial per axis-0 CTA in `part`, at least g.P entries).
+bool cg_pq_fusable(const bri17_op* op);
+int apply_stiffness_cg_async(bri17_op* op, const float* p, float* q, bri17gb::CgState* st,
+                             double* part, cudaStream_t stream);
 
 // Batched forms used by the server: `batch` fields of one geometry,
 // contiguous (entry z at z * dim * size), with per-entry material

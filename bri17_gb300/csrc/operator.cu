@@ -516,9 +516,16 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
     const int form = env_form >= 0 ? env_form : fp.form;
     if constexpr (std::is_same<T, float>::value && DIM == 3) {
       if ((form == 2 || form == 3) &&
-          ct_axis0_stiffness_tma_f32(p.n, form == 3, X, g.P, g.cspec, bstride, batch, fp, mask,
-                                     st))
+          ct_axis0_stiffness_tma_f32(p.n, form == 3 && !fp.cg, X, g.P, g.cspec, bstride, batch,
+                                     fp, mask, st))
         return BRI17_OK;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+      // cg_pq_fusable admits only layouts the TMA-staged form takes.
+      if (fp.cg) {
+        set_error("internal: p.Kp in the stiffness pass needs the TMA-staged form");
+        return BRI17_ERR_UNSUPPORTED_SIZE;
+      }
     }
     if (form == 1 &&
         ct_axis0_stiffness_staged<T, DIM>(p.n, X, g.P, g.cspec, bstride, batch, fp, mask, st))
@@ -572,6 +579,12 @@ static FusedParams<T> fused_params(const bri17_op* op, const Tables<T>& tab,
   fp.mat = nullptr;
   fp.form = op->fused_form;
   fp.status = op->status_dev;
+  if constexpr (std::is_same<T, float>::value) {
+    if (mode == kModeStiffness) {
+      fp.cg = op->cg_st;
+      fp.cg_part = op->cg_part;
+    }
+  }
   return fp;
 }
 
@@ -746,6 +759,27 @@ int apply_stiffness_async(bri17_op* op, const void* u, void* f,
         op, op->tab64, (const double*)u, (double*)f, 1, op->spec, nullptr, st);
   return run_pipeline<float, kModeStiffness>(
       op, op->tab32, (const float*)u, (float*)f, 1, op->spec, nullptr, st);
+}
+
+bool cg_pq_fusable(const bri17_op* op) {
+  const Geometry& g = op->g;
+  if (op->precision != BRI17_F32 || g.dim != 3 || !g.use_p8[0] || !g.use_p8_row) return false;
+  const int env_form = env_fused_form();
+  if ((env_form >= 0 ? env_form : op->fused_form) != 2) return false;
+  if (g.n[0] < 16 || g.n[0] > 1024) return false;
+  return tma_layout_ok<float>(op->spec, g.P, g.cspec, 3 * g.cspec, g.n[0]);
+}
+
+int apply_stiffness_cg_async(bri17_op* op, const float* p, float* q, CgState* st, double* part,
+                             cudaStream_t s) {
+  int rc = ensure_spectrum(op, op->g.dim);
+  if (rc != BRI17_OK) return rc;
+  op->cg_st = st;
+  op->cg_part = part;
+  rc = run_pipeline<float, kModeStiffness>(op, op->tab32, p, q, 1, op->spec, nullptr, s);
+  op->cg_st = nullptr;
+  op->cg_part = nullptr;
+  return rc;
 }
 
 int apply_stiffness_batched_async(bri17_op* op, int batch, const void* u,

@@ -40,6 +40,8 @@ struct BatchMask {
   }
 };
 
+struct CgState;
+
 template <typename T>
 struct FusedParams {
   Tables<T> tab;
@@ -52,6 +54,11 @@ struct FusedParams {
   const T* mat;     // optional per-batch (s, mu) pairs, overriding s, mu
   int form;         // power-of-two axis-0 stiffness pass: 0 registers, 1 staged
   int* status;      // the handle's status words (mapped host memory) or null
+  // A CG iteration's p.Kp, summed by Parseval in the FP32 TMA-staged
+  // stiffness pass (axis0_stiffness_tma with PQ) into `cg` (pq, alpha) with
+  // one partial per CTA in cg_part; null outside CG iterations.
+  CgState* cg = nullptr;
+  double* cg_part = nullptr;
 };
 
 // ---------------------------------------------------------------------------

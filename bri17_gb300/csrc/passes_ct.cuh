@@ -225,6 +225,10 @@ int tma_pitch() {
   return exchange_pitch(N, tma_lines<T>(N), (int)sizeof(cplx<T>), true);
 }
 
+// Shared memory the p.Kp reduction of the PQ instance adds after the
+// mbarrier: 8 warp sums and the last-CTA flag.
+constexpr size_t kTmaPqSmem = 80;
+
 template <typename T, int N>
 size_t tma_smem_bytes() {
   constexpr int TB = tma_lines<T>(N);
@@ -241,11 +245,7 @@ bool ct_axis0_stiffness_tma(int n0, bool keep, cplx<T>* X, int64_t P, int64_t cs
   constexpr int kPer = (int)(sizeof(cplx<T>) / sizeof(T));
   // The map's strides (P and cstride complex) must be multiples of 16
   // bytes, the base 16-byte aligned, and the planes evenly spaced.
-  if ((P * (int64_t)sizeof(cplx<T>)) % 16 != 0 || cstride != (int64_t)n0 * P ||
-      bstride != DIM * cstride)
-    return false;
-  if (reinterpret_cast<uintptr_t>(X) % 16 != 0) return false;
-  if ((int64_t)P * kPer >= ((int64_t)1 << 31)) return false;
+  if (!tma_layout_ok<T>(X, P, cstride, bstride, n0)) return false;
   switch (n0) {
 #define CASE(N)                                                                          \
   case N: {                                                                           \
@@ -269,6 +269,15 @@ bool ct_axis0_stiffness_tma(int n0, bool keep, cplx<T>* X, int64_t P, int64_t cs
         launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, true>, grid, TT * TB,        \
                    tma_smem_bytes<T, N>(), st, map, P, TB, tma_pitch<T, N>(),            \
                    CtEng<N, E>{}, fp, mask);                                             \
+        launched = true;                                                                 \
+      }                                                                                  \
+    }                                                                                    \
+    if constexpr (std::is_same<T, float>::value) {                                       \
+      if (!launched && fp.cg) {                                                          \
+        if (batch != 1) return false;                                                    \
+        launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, false, true>, grid, TT * TB, \
+                   tma_smem_bytes<T, N>() + kTmaPqSmem, st, map, P, TB,                  \
+                   tma_pitch<T, N>(), CtEng<N, E>{}, fp, mask);                          \
         launched = true;                                                                 \
       }                                                                                  \
     }                                                                                    \
@@ -297,6 +306,10 @@ void ct_set_smem_attrs_tma(size_t max_smem) {
       cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, true>,                 \
                            cudaFuncAttributeMaxDynamicSharedMemorySize,                  \
                            (int)std::min(max_smem, tma_smem_bytes<T, N>()));             \
+    if constexpr (std::is_same<T, float>::value)                                         \
+      cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, false, true>,          \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,                  \
+                           (int)std::min(max_smem, tma_smem_bytes<T, N>() + kTmaPqSmem)); \
   }
   CASE(16) CASE(32) CASE(64) CASE(128) CASE(256) CASE(512) CASE(1024)
 #undef CASE

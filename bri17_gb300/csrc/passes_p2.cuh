@@ -11,6 +11,7 @@
 #include "fft8_ct.cuh"
 #include "passes.cuh"
 #include "pdl.cuh"
+#include "reduce.cuh"
 #include "tma.cuh"
 
 namespace bri17gb {
@@ -551,6 +552,62 @@ __global__ void __launch_bounds__(kP2Threads)
   }
 }
 
+// p.Kp of a CG iteration from the stiffness pass, by Parseval: with the
+// unnormalised forward transform and K(k) carrying the inverse's 1/|N|,
+// sum_x p(x) (K p)(x) = sum over the half spectrum of w Re(conj(p^) (K p)^),
+// w = 1 on the k_last = 0 and Nyquist lines (even last axis) and 2 elsewhere.
+// Each CTA reduces its threads' sums (`part`, already without w; `w` the
+// line's weight) through `red` (9 doubles of shared memory) into one partial
+// per CTA; the last CTA to finish adds the partials in index order (the
+// result does not depend on the order the CTAs ran in), sets pq and
+// alpha = rr / pq, or flags a breakdown when pq is not positive and finite,
+// while the CG is active.  Every thread of the CTA calls it.
+template <typename T>
+__device__ __forceinline__ void cg_pq_reduce(float part, double w, const FusedParams<T>& fp,
+                                             double* red) {
+  const int nwarps = (int)(blockDim.x >> 5), lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double v = w * (double)part;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  int* last = reinterpret_cast<int*>(red + 8);
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int i = 0; i < nwarps; i++) b += red[i];
+    fp.cg_part[blockIdx.x] = b;
+    __threadfence();
+    const unsigned t = atomicAdd(&fp.cg->counter, 1u);
+    *last = t == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (*last) {
+    __threadfence();
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(fp.cg_part + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __syncthreads();
+    if (lane == 0) red[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.0;
+      for (int i = 0; i < nwarps; i++) tot += red[i];
+      CgState* st = fp.cg;
+      if (st->active) {
+        st->pq = tot;
+        if (!(tot > 0.0) || !isfinite(tot)) {
+          st->flag = BRI17_ERR_BREAKDOWN;
+          st->active = 0;
+        } else {
+          st->alpha = st->rr / tot;
+        }
+      }
+      st->counter = 0u;
+    }
+  }
+}
+
 // Bounded mbarrier waits that ran out in this translation unit's TMA kernels.
 static __device__ int g_tma_timeouts;
 // Limit of the first wait on a tile's copies (ns of global time).
@@ -571,7 +628,7 @@ static __device__ unsigned long long g_tma_wait_limit_ns = kWaitLimitNs;
 // registers at a time); true keeps all DIM components in registers from the
 // forward transforms through K(k) u(k) to the inverse ones (fewer
 // shared-memory round trips, more registers).
-template <typename T, int DIM, class Eng, bool KEEP>
+template <typename T, int DIM, class Eng, bool KEEP, bool PQ = false>
 __global__ void __launch_bounds__(256)
     axis0_stiffness_tma(const __grid_constant__ CUtensorMap map, int64_t P, int TB, int pitch,
                         Eng p0, FusedParams<T> fp, BatchMask mask) {
@@ -592,7 +649,13 @@ __global__ void __launch_bounds__(256)
   if (threadIdx.x == 0) mbar_init(bar, 1);
   p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();
-  if (mask.skip(blockIdx.y)) return;
+  // A CTA that leaves early still takes its part in the p.Kp reduction (a
+  // zero), so that the last CTA is found and the ticket counter returns to 0.
+  double* red = reinterpret_cast<double*>(bar + 1);
+  if (mask.skip(blockIdx.y)) {
+    if constexpr (PQ) cg_pq_reduce<T>(0.f, 0.0, fp, red);
+    return;
+  }
   // The copy destinations must be 128-byte aligned; the launch guarantees
   // it, and a misplaced window skips the CTA with an error count.
   if (smem_addr(tile) & 127u) {
@@ -600,6 +663,7 @@ __global__ void __launch_bounds__(256)
       atomicAdd(&g_tma_timeouts, 1);
       report_status(fp.status, 1);
     }
+    if constexpr (PQ) cg_pq_reduce<T>(0.f, 0.0, fp, red);
     return;
   }
   __syncthreads();
@@ -637,6 +701,7 @@ __global__ void __launch_bounds__(256)
       report_status(fp.status, 0);
       mbar_wait(bar, 0, kWaitLimitNs);
     }
+    if constexpr (PQ) cg_pq_reduce<T>(0.f, 0.0, fp, red);
     return;
   }
   cplx<T>* buf = exch + tb * pitch;
@@ -678,6 +743,8 @@ __global__ void __launch_bounds__(256)
     // the tile (their registers are the constraint: the same change made
     // that pass slower, 80 -> 92 us at 128^3).
     constexpr bool KL = std::is_same<T, float>::value;
+    static_assert(!PQ || KL, "p.Kp by Parseval: FP32 only");
+    float pq = 0.f;  // this thread's modes' Re(conj(p) . K p), PQ only
     cplx<T> v[Eng::E];
 #pragma unroll 1
     for (int c = 0; c < DIM; c++) {
@@ -700,11 +767,22 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int c = 0; c < DIM - 1; c++) u[c] = tile[((size_t)c * n0 + k0) * TB + tb];
         u[DIM - 1] = v[q];
+        cplx<T> u0[DIM];
+        if constexpr (PQ) {
+#pragma unroll
+          for (int c = 0; c < DIM; c++) u0[c] = u[c];
+        }
         stiffness_lf<T, DIM>(phi0, chi0, psi0, lf, s, mu, u);
+        if constexpr (PQ) {
+#pragma unroll
+          for (int c = 0; c < DIM; c++) pq = fmaf(u0[c].x, u[c].x, fmaf(u0[c].y, u[c].y, pq));
+        }
 #pragma unroll
         for (int c = 0; c < DIM - 1; c++) tile[((size_t)c * n0 + k0) * TB + tb] = u[c];
         v[q] = u[DIM - 1];
       }
+      if constexpr (PQ)
+        cg_pq_reduce<T>(pq, valid ? (k2 == 0 || k2 == fp.H - 1 ? 1.0 : 2.0) : 0.0, fp, red);
     } else {
 #pragma unroll 2
       for (int q = 0; q < Eng::E; q++) {
@@ -740,6 +818,16 @@ __global__ void __launch_bounds__(256)
         tma_store_3d(&map, x0, r0, z * DIM + c, tile + ((size_t)c * n0 + r0) * TB);
     tma_store_commit_and_wait();
   }
+}
+
+// The tensor-copy layout the TMA-staged axis-0 launcher needs (false: it
+// declines, launching nothing).
+template <typename T>
+inline bool tma_layout_ok(const void* X, int64_t P, int64_t cstride, int64_t bstride, int n0) {
+  constexpr int kPer = (int)(sizeof(cplx<T>) / sizeof(T));
+  return (P * (int64_t)sizeof(cplx<T>)) % 16 == 0 && cstride == (int64_t)n0 * P &&
+         bstride == 3 * cstride && reinterpret_cast<uintptr_t>(X) % 16 == 0 &&
+         (int64_t)P * kPer < ((int64_t)1 << 31);
 }
 
 // Launchers of the compile-time-length kernels (passes_ct.cuh, instantiated

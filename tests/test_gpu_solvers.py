@@ -238,3 +238,28 @@ def test_mixed_cg_matches_oracle_and_is_deterministic(shape, L):
     assert e1 <= max(4 * ep, 1e-8), (e1, ep)
     # About as many iterations as plain CG (reliable updates keep p).
     assert i1["iterations"] <= 1.3 * ip["iterations"] + 16, (i1, ip)
+
+
+@pytest.mark.parametrize("shape", [(64, 64, 128), (128, 32, 16)])
+def test_fp32_cg_with_pq_in_the_stiffness_pass(shape):
+    """With the TMA-staged axis-0 form, the FP32 CG sums p.Kp by Parseval in
+    the stiffness pass (no separate pass over p and q); with the staged form
+    it runs the separate reduction.  Both converge alike, land equally close
+    to the oracle, and repeat bit for bit (fixed-order reductions)."""
+    L = (1.0, 0.9, 1.1)
+    h32, ho = pair(shape, L, 1.0, 0.3, precision="f32")
+    h64, _ = pair(shape, L, 1.0, 0.3)
+    tau = np.random.default_rng(11).standard_normal((6,) + shape)
+    b = h64.eigenstress_rhs(to_dev(tau))
+    x_ref = O.eigenstress_solve_half(ho, tau, workers=4)
+    res = {}
+    for form in ("tma", "staged"):
+        h32.fused_form = form
+        x1, i1 = h32.cg_solve(b, tol=1e-5, mode="plain")
+        x2, i2 = h32.cg_solve(b, tol=1e-5, mode="plain")
+        assert i1["status"] == 0 and i1["rel_residual"] <= 1e-5, (form, i1)
+        assert bool((x1 == x2).all()) and i1["iterations"] == i2["iterations"], form
+        res[form] = (rel_l2(x1.cpu().numpy(), x_ref), i1["iterations"])
+    (et, it_t), (es, it_s) = res["tma"], res["staged"]
+    assert et <= max(2 * es, 1e-4), (et, es)
+    assert abs(it_t - it_s) <= 0.1 * it_s + 4, (it_t, it_s)
