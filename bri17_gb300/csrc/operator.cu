@@ -672,7 +672,6 @@ static int run_pipeline(bri17_op* op, const Tables<T>& tab, const T* in,
   cplx<T>* S = reinterpret_cast<cplx<T>*>(spec);
   const int64_t bstride = (int64_t)cmax * g.cspec;
   set_smem_attrs<T>();
-  PdlScope chain(pdl_for_entries((int64_t)batch * cmax * g.cspec));
   // Launch over entries [z0, z0 + nz): one launch when their data are
   // contiguous (c == cmax or a single entry), else one per entry.
   auto mask_at = [&](int z0, int64_t unit) {
@@ -1418,7 +1417,6 @@ static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
   none.unit = 1;
   const int nl = g.n[dim - 1];
   const int64_t rows = (int64_t)dim * (g.size / nl);
-  PdlScope chain(pdl_for_entries((int64_t)dim * g.cspec));
   bool ok;
   {
     PassScope ps(op, 0, st);

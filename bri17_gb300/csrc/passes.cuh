@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kThreads)
   const int m = even ? n / 2 : n;
   const int64_t row0 = (int64_t)blockIdx.x * rows_per_cta;
   const int nr = (int)min((int64_t)rows_per_cta, nrows - row0);
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
   pdl_wait();
   if (mask.skip(row0)) return;
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kThreads)
   const int m = even ? n / 2 : n;
   const int64_t row0 = (int64_t)blockIdx.x * rows_per_cta;
   const int nr = (int)min((int64_t)rows_per_cta, nrows - row0);
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
   __syncthreads();
   pdl_wait();
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t b0 = (int64_t)blockIdx.x * TB;
   const int nb = (int)min((int64_t)TB, B - b0);
   cplx<T>* base = X + (int64_t)blockIdx.y * n * B + b0;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = tw_g[t];
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t b0 = (int64_t)blockIdx.x * TB;
   const int nb = (int)min((int64_t)TB, P - b0);
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b0;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   for (int t = threadIdx.x; t < n0; t += blockDim.x) tw[t] = fp.tab.tw[0][t];
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kP2Threads, RowCtas<T>::value)
   const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   pm.template load_tw<T>(tw, tw_g, n, 2);
   for (int i = threadIdx.x; i <= m; i += blockDim.x) {
     const cplx<T> w = tw_g[i];
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kP2Threads)
   const int t = threadIdx.x % TT, rb = threadIdx.x / TT;
   const int64_t row = row0 + rb;
   const bool valid = rb < RB && row < nrows;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
   if constexpr (Eng::template stage<T>()) pm.template load_tw<T>(stw, tw_g, n, 2);
   __syncthreads();
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kP2Threads)
   const int64_t a = line / B;
   bool valid = line < nlines;
   cplx<T>* base = X + a * n * B + (line - a * B);
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   p.template load_tw<T>(tw, tw_g, n, 1);
   pdl_wait();
   if (mask.flags) {
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kP2FusedThreads)
   const int64_t b = (int64_t)blockIdx.x * TB + tb;
   const bool valid = b < P;
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(kP2Threads)
   const int64_t b = (int64_t)blockIdx.x * TB + tb;
   const bool valid = b < P;
   cplx<T>* base = X + (int64_t)blockIdx.y * bstride + b;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();
   if (mask.skip(blockIdx.y)) return;
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(256)
   const int64_t b = (int64_t)blockIdx.x * TB + tb;
   const int x0 = (int)((int64_t)blockIdx.x * TB * kPer);
   const int z = blockIdx.y;
-  pdl_launch_dependents();
+  pdl_launch_dependents<T>();
   if (threadIdx.x == 0) mbar_init(bar, 1);
   p0.template load_tw<T>(tw, fp.tab.tw[0], n0, 1);
   pdl_wait();

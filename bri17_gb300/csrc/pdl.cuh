@@ -1,71 +1,54 @@
 // pdl.cuh -- programmatic dependent launch for the operator's passes.
 //
 // The passes of one operator application are launched back to back on one
-// stream, each with cudaLaunchAttributeProgrammaticStreamSerialization.  A
-// pass signals `griddepcontrol.launch_dependents` at its start, so the next
-// pass is launched as soon as every CTA of this one is resident; the next
-// pass then loads its constant tables into shared memory and executes
+// stream, each with cudaLaunchAttributeProgrammaticStreamSerialization, so
+// the next pass's launch is prepared while the previous one runs.  The next
+// pass loads its constant tables into shared memory and then executes
 // `griddepcontrol.wait` -- which returns when the previous grid has
 // completed and its memory is visible -- before it reads or writes any
-// field.  The launch latency and table set-up of each pass overlap the tail
-// of the previous one.  Without the attribute both instructions are no-ops.
+// field.  When the previous pass triggers early (`launch_dependents` at the
+// start of its CTAs, FP64 passes; see below), the next pass's CTAs start
+// while the previous pass's last CTAs still run; otherwise as those exit.
+// Without the attribute both instructions are no-ops.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <utility>
 
 namespace bri17gb {
 
+// Early trigger, for FP64 passes only.  With it a pass lets the next one
+// launch as soon as all of its CTAs are running, so the next pass's CTAs
+// become resident during this pass's tail.  Without it the next pass
+// launches as this pass's CTAs exit (still ahead of a plain stream launch).
+// Measured on the GB300, the early trigger pays for the FP64 passes, which
+// are bound by the FP64 pipe (128^3: 0.928 -> 0.925 ms per application).
+// For the memory-bound FP32 passes and the float-pair passes it slowed the
+// tails: FP32 256^3 0.515 ms against 0.446 ms without it, 512x512x128
+// 1.187 against 0.974 ms; float pairs at 128^3 25.6 against 25.8 GDoF/s.
+template <typename T>
 __device__ __forceinline__ void pdl_launch_dependents() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if constexpr (std::is_same<T, double>::value)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 __device__ __forceinline__ void pdl_wait() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
-// Which pass sequences are chained.  Measured on the GB300 (FP32 operator,
-// five passes): chaining hides the launch latency of short passes (128^3:
-// 0.098 -> 0.061 ms per application; FP64 and float pairs at 128^3 gain
-// 1.5% and 4.5%), but slows the passes over large spectra (256^3: 0.460 ->
-// 0.515 ms; 512x512x128: 0.985 -> 1.184 ms, the passes themselves running
-// slower).  So a sequence is chained when each of its passes moves at most
-// kPdlMaxEntries complex spectrum entries (all components and batch
-// entries).  BRI17_PDL=0 or =1 forces plain or chained launches (for
-// measurements).
-constexpr int64_t kPdlMaxEntries = int64_t(8) << 20;
-
-inline int pdl_env_mode() {
-  static const int mode = [] {
+// BRI17_PDL=0 launches the passes without the attribute (plain stream
+// order; for measurements).
+inline bool pdl_enabled() {
+  static const bool on = [] {
     const char* e = getenv("BRI17_PDL");
-    if (!e) return -1;
-    return strcmp(e, "0") == 0 ? 0 : strcmp(e, "1") == 0 ? 1 : -1;
+    return !(e && strcmp(e, "0") == 0);
   }();
-  return mode;
-}
-
-inline bool pdl_for_entries(int64_t entries) {
-  const int m = pdl_env_mode();
-  return m >= 0 ? m == 1 : entries <= kPdlMaxEntries;
-}
-
-// The calling thread's choice for the launches it makes (set by PdlScope
-// around one pass sequence).
-inline bool& pdl_thread_flag() {
-  thread_local bool on = true;
   return on;
 }
-
-struct PdlScope {
-  bool prev;
-  explicit PdlScope(bool on) : prev(pdl_thread_flag()) { pdl_thread_flag() = on; }
-  ~PdlScope() { pdl_thread_flag() = prev; }
-  PdlScope(const PdlScope&) = delete;
-  PdlScope& operator=(const PdlScope&) = delete;
-};
 
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
@@ -79,7 +62,7 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = pdl_thread_flag() ? 1 : 0;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
