@@ -167,8 +167,7 @@ __device__ __forceinline__ float df_pow2(int e) {
   return __int_as_float(1 << (e + 149));
 }
 
-template <>
-__device__ __forceinline__ df64 from_io<df64>(double v) {
+static __device__ __noinline__ df64 df_from_double_general(double v) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int ex = (int)((bits >> 52) & 0x7FF);
   const bool neg = (bits >> 63) != 0;
@@ -211,8 +210,7 @@ __device__ __forceinline__ df64 from_io<df64>(double v) {
 // the 53 are dropped: error below 2^-52 relative), then one normalisation.
 // Zero or subnormal hi gives a signed zero; an infinite or NaN part gives
 // infinity or NaN.
-template <>
-__device__ __forceinline__ double to_io<df64>(df64 v) {
+static __device__ __noinline__ double df_to_double_general(df64 v) {
   const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
   const int eh = (int)((hb >> 23) & 0xFF), el = (int)((lb >> 23) & 0xFF);
   unsigned long long sign = (unsigned long long)(hb >> 31) << 63;
@@ -242,6 +240,73 @@ __device__ __forceinline__ double to_io<df64>(df64 v) {
   if (e >= 0x7FF) return __longlong_as_double((long long)(sign | (0x7FFull << 52)));
   return __longlong_as_double(
       (long long)(sign | ((unsigned long long)e << 52) | ((unsigned long long)M & ((1ull << 52) - 1))));
+}
+
+// Fast paths of the conversions, 32-bit integer operations only (the
+// general forms above work on 64-bit integers and normalise with variable
+// shifts; on the FP64 operator's 128^3 fields they took about a tenth of the
+// float-pair application).
+//
+// double -> hi + lo for biased exponents E in [949, 1149] (|v| in about
+// [2^-74, 2^126]): hi's 23 fraction bits are the double's top 23, rounded to
+// nearest even on the 29 below (the carry of the rounding increment runs
+// into hi's exponent as it should); the signed remainder (|r| <= 2^28)
+// converts to a float rounded to nearest and is scaled by 2^(E - 1075),
+// a normal power of two in this range.  Same values as the general form.
+template <>
+__device__ __forceinline__ df64 from_io<df64>(double v) {
+  const unsigned h = (unsigned)__double2hiint(v), l = (unsigned)__double2loint(v);
+  const unsigned E = (h >> 20) & 0x7FFu;
+  if (E < 949u || E > 1149u) return df_from_double_general(v);
+  const unsigned sign = h & 0x80000000u;
+  const unsigned frac = ((h & 0xFFFFFu) << 3) | (l >> 29);
+  const unsigned r = l & 0x1FFFFFFFu;
+  const unsigned up = (r > 0x10000000u || (r == 0x10000000u && (frac & 1u))) ? 1u : 0u;
+  const float hi = __uint_as_float((sign | ((E - 896u) << 23) | frac) + up);
+  const int rem = (int)r - (up ? 0x20000000 : 0);
+  float lo = __fmul_rn(__int2float_rn(rem), __uint_as_float((E - 948u) << 23));
+  if (sign) lo = -lo;
+  return df64(hi, lo);
+}
+
+// hi + lo -> double for a normalised pair (|lo| <= ulp(hi)/2, so lo sits at
+// least 24 binades below hi) of normal floats, or a zero lo.  With
+// s = e_hi - e_lo, M = m_hi 2^29 +- m_lo 2^(29 - s) in units of the double's
+// last place: exact for s <= 29; for s >= 30 lo's bits below that place are
+// dropped (|lo| truncated), as in the general form.  Only the case M < 2^52
+// (hi a power of two, lo of the other sign) needs a left shift, exact for
+// s <= 29; for s >= 30 it goes to the general form, as do specials,
+// subnormal parts and pairs that are not normalised.  Same values as the
+// general form.
+template <>
+__device__ __forceinline__ double to_io<df64>(df64 v) {
+  const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const unsigned eh = (hb >> 23) & 0xFFu, el = (lb >> 23) & 0xFFu;
+  const unsigned long long mh = (unsigned long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
+  const unsigned sign_hi = hb & 0x80000000u;
+  const unsigned s = eh - el;
+  const bool lo_zero = (lb << 1) == 0u;
+  if (eh - 1u >= 254u || (!lo_zero && (el - 1u >= 254u || s < 24u)))
+    return df_to_double_general(v);
+  unsigned L = 0u;
+  if (!lo_zero) {
+    const unsigned ml = (lb & 0x7FFFFFu) | 0x800000u;
+    if (s <= 29u) {
+      L = ml << (29u - s);
+    } else {
+      L = ml >> (s - 29u < 31u ? s - 29u : 31u);
+    }
+  }
+  const bool neg = ((hb ^ lb) >> 31) && !lo_zero;
+  unsigned long long M = neg ? mh - L : mh + L;
+  unsigned E = eh + 896u;
+  if (M < (1ull << 52)) {
+    if (s > 29u) return df_to_double_general(v);
+    M <<= 1;
+    E -= 1u;
+  }
+  return __hiloint2double((int)(sign_hi | (E << 20) | (unsigned)((M >> 32) & 0xFFFFFu)),
+                          (int)(unsigned)M);
 }
 
 // Complex products of float pairs: each part is one df_dot2 (the generic

@@ -362,6 +362,34 @@ def test_float_pair_operator_matches_oracle(shape, L, mu, nu):
     assert torch.equal(h.apply_stiffness(ud), f64)
 
 
+def test_float_pair_conversions_across_the_range():
+    """Doubles outside the conversions' fast range (zeros, magnitudes below
+    2^-74) take the general integer conversions, the rest the fast ones;
+    both kinds sit in one field.  Each component of the float-pair output
+    stays within 1e-13 of the FP64 operator's."""
+    import torch
+    shape = (64, 64, 128)
+    h, _ = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.3)
+    rng = np.random.default_rng(23)
+    u = rng.standard_normal((3,) + shape)
+    sel = rng.random(u.shape)
+    u[sel < 0.05] = 0.0
+    u[(sel >= 0.05) & (sel < 0.10)] *= 1e-28           # below 2^-74: general
+    u[(sel >= 0.10) & (sel < 0.15)] *= 2.0 ** -70      # just inside the fast range
+    u[(sel >= 0.15) & (sel < 0.16)] *= 2.0 ** 40       # large, well inside the range
+    ud = to_dev(u)
+    f64 = h.apply_stiffness(ud)
+    h.set_float_pair(True)
+    try:
+        f = h.apply_stiffness(ud)
+        torch.cuda.synchronize()
+    finally:
+        h.set_float_pair(False)
+    assert bool(torch.isfinite(f).all())
+    for k in range(3):
+        assert float((f[k] - f64[k]).norm() / f64[k].norm()) <= 1e-13, k
+
+
 def test_float_pair_host_buffers_and_rejected_grids():
     import torch
     from bri17_gb300._lib import Bri17Error
