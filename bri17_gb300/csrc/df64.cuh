@@ -271,42 +271,33 @@ __device__ __forceinline__ df64 from_io<df64>(double v) {
 
 // hi + lo -> double for a normalised pair (|lo| <= ulp(hi)/2, so lo sits at
 // least 24 binades below hi) of normal floats, or a zero lo.  With
-// s = e_hi - e_lo, M = m_hi 2^29 +- m_lo 2^(29 - s) in units of the double's
-// last place: exact for s <= 29; for s >= 30 lo's bits below that place are
-// dropped (|lo| truncated), as in the general form.  Only the case M < 2^52
-// (hi a power of two, lo of the other sign) needs a left shift, exact for
-// s <= 29; for s >= 30 it goes to the general form, as do specials,
-// subnormal parts and pairs that are not normalised.  Same values as the
-// general form.
+// s = e_hi - e_lo, lo is m_lo 2^(29 - s) units of the double's last place
+// in hi's binade: exact for s <= 29; for s >= 30 lo's bits below that place
+// are dropped (|lo| truncated), as in the general form.  That many units
+// are added to or taken from hi's double bit pattern, which stays in hi's
+// binade unless hi is a power of two and lo has the other sign; that case,
+// specials, subnormal parts and pairs that are not normalised go to the
+// general form.  Same values as the general form.
 template <>
 __device__ __forceinline__ double to_io<df64>(df64 v) {
   const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
   const unsigned eh = (hb >> 23) & 0xFFu, el = (lb >> 23) & 0xFFu;
-  const unsigned long long mh = (unsigned long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
-  const unsigned sign_hi = hb & 0x80000000u;
   const unsigned s = eh - el;
   const bool lo_zero = (lb << 1) == 0u;
-  if (eh - 1u >= 254u || (!lo_zero && (el - 1u >= 254u || s < 24u)))
+  const bool neg = ((hb ^ lb) >> 31) != 0u;
+  // hi as a double: sign, exponent rebased by 1023 - 127 = 896, the 23
+  // fraction bits at the top of the 52.
+  const unsigned long long dh =
+      ((unsigned long long)((hb & 0x80000000u) | (((hb & 0x7FFFFFFFu) >> 3) + (896u << 20)))
+       << 32) |
+      (unsigned long long)((hb & 7u) << 29);
+  if (eh - 1u >= 254u) return df_to_double_general(v);
+  if (lo_zero) return __longlong_as_double((long long)dh);
+  if (el - 1u >= 254u || s < 24u || (neg && (hb & 0x7FFFFFu) == 0u))
     return df_to_double_general(v);
-  unsigned L = 0u;
-  if (!lo_zero) {
-    const unsigned ml = (lb & 0x7FFFFFu) | 0x800000u;
-    if (s <= 29u) {
-      L = ml << (29u - s);
-    } else {
-      L = ml >> (s - 29u < 31u ? s - 29u : 31u);
-    }
-  }
-  const bool neg = ((hb ^ lb) >> 31) && !lo_zero;
-  unsigned long long M = neg ? mh - L : mh + L;
-  unsigned E = eh + 896u;
-  if (M < (1ull << 52)) {
-    if (s > 29u) return df_to_double_general(v);
-    M <<= 1;
-    E -= 1u;
-  }
-  return __hiloint2double((int)(sign_hi | (E << 20) | (unsigned)((M >> 32) & 0xFFFFFu)),
-                          (int)(unsigned)M);
+  const unsigned ml = (lb & 0x7FFFFFu) | 0x800000u;
+  const unsigned L = s <= 29u ? ml << (29u - s) : ml >> (s - 29u < 31u ? s - 29u : 31u);
+  return __longlong_as_double((long long)(neg ? dh - L : dh + L));
 }
 
 // Complex products of float pairs: each part is one df_dot2 (the generic
