@@ -58,13 +58,23 @@ struct Geometry {
   Plan8 p8[3];
   bool use_p8_row;
   bool use_p8[3];
+  // Lengths 3 * 2^k: the compile-time twelve-element engine (CtEng3) where
+  // it has an instance, else the generic engine.
+  bool use_ct3_row;
+  bool use_ct3[3];
 };
+
+inline bool is_3pow2(int n) { return n > 0 && n % 3 == 0 && is_pow2(n / 3) && n / 3 >= 8; }
 
 // Fill the register-resident plans of a geometry whose n, dim are set.
 inline void set_p8_plans(Geometry* g) {
   const int nl = g->n[g->dim - 1];
   g->use_p8_row = (nl % 2 == 0) && make_plan8(nl / 2, &g->p8_row);
-  for (int i = 0; i < 3; i++) g->use_p8[i] = i < g->dim && make_plan8(g->n[i], &g->p8[i]);
+  g->use_ct3_row = (nl % 2 == 0) && is_3pow2(nl / 2);
+  for (int i = 0; i < 3; i++) {
+    g->use_p8[i] = i < g->dim && make_plan8(g->n[i], &g->p8[i]);
+    g->use_ct3[i] = i < g->dim && is_3pow2(g->n[i]);
+  }
 }
 
 bool make_plan(int n, AxisPlan* p);

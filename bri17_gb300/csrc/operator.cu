@@ -231,6 +231,7 @@ static void set_smem_attrs() {
     cudaFuncSetAttribute(axis0_stiffness_p2<T, 2, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     cudaFuncSetAttribute(axis0_stiffness_p2<T, 3, RtEng>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     ct_set_smem_attrs(kMaxSmem);
+    if constexpr (!std::is_same<T, df64>::value) ct3_set_smem_attrs_t<T>(kMaxSmem);
 #define SET_FUSED(D, M) \
   cudaFuncSetAttribute(axis0_fused<T, D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem)
     SET_FUSED(2, kModeStiffness);
@@ -270,6 +271,9 @@ template <typename T>
 static int launch_rows_r2c(const Geometry& g, const T* x, cplx<T>* X,
                            int64_t nrows, const Tables<T>& tab, BatchMask mask,
                            cudaStream_t st) {
+  if (g.use_ct3_row && ct3_rows_r2c<T>(g.n[g.dim - 1] / 2, x, X, nrows, g.H,
+                                       tab.tw[g.dim - 1], mask, st))
+    return BRI17_OK;
   if (g.use_p8_row) {
     const Plan8& p = g.p8_row;
     if (ct_rows_r2c<T>(p.n, x, X, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
@@ -295,6 +299,9 @@ template <typename T>
 static int launch_rows_c2r(const Geometry& g, const cplx<T>* X, T* x,
                            int64_t nrows, const Tables<T>& tab, BatchMask mask,
                            cudaStream_t st) {
+  if (g.use_ct3_row && ct3_rows_c2r<T>(g.n[g.dim - 1] / 2, X, x, nrows, g.H,
+                                       tab.tw[g.dim - 1], mask, st))
+    return BRI17_OK;
   if (g.use_p8_row) {
     const Plan8& p = g.p8_row;
     if (ct_rows_c2r<T>(p.n, X, x, nrows, g.H, tab.tw[g.dim - 1], mask, st)) return BRI17_OK;
@@ -341,7 +348,7 @@ int access_wavefronts(const int* byte_addr, int lanes, int csize) {
 
 // Stage schedule of the engines: E = 8 as make_plan8 (8s, then 4 x 4 or
 // 4); E = 16 as the compile-time engine's (16s, then one stage of the
-// remaining power of two).
+// remaining power of two); E = 12 for 3 * 2^k (4s, a 2, the 3 last).
 struct StagePlan {
   int T, nst, radix[12];
 };
@@ -353,6 +360,18 @@ bool stage_plan(int n, int E, StagePlan* sp) {
     sp->T = p.T;
     sp->nst = p.nst;
     for (int s = 0; s < p.nst; s++) sp->radix[s] = p.radix[s];
+    return true;
+  }
+  if (E == 12) {
+    // PE3: radix 4s, one 2 when log2(n / 3) is odd, the 3 last.
+    if (!is_3pow2(n) || n > 768) return false;
+    int lp = 0;
+    while ((1 << lp) < n / 3) lp++;
+    sp->T = n / 12;
+    sp->nst = 0;
+    for (int s = 0; s < lp / 2; s++) sp->radix[sp->nst++] = 4;
+    if (lp % 2) sp->radix[sp->nst++] = 2;
+    sp->radix[sp->nst++] = 3;
     return true;
   }
   if (E != 16 || !is_pow2(n) || n < 16 || n > 1024) return false;
@@ -462,6 +481,8 @@ bool encode_tiled_map_3d(CUtensorMap* map, const void* base, int elem_bytes, uin
 template <typename T, bool INV>
 static int launch_axis1(const Geometry& g, cplx<T>* X, int64_t nouter,
                         const Tables<T>& tab, BatchMask mask, cudaStream_t st) {
+  if (g.use_ct3[1] && ct3_axis_c2c<T, INV>(g.n[1], X, g.H, nouter, tab.tw[1], mask, st))
+    return BRI17_OK;
   if (g.use_p8[1]) {
     const Plan8& p = g.p8[1];
     if (ct_axis_c2c<T, INV>(p.n, X, g.H, nouter, tab.tw[1], mask, st)) return BRI17_OK;
@@ -540,6 +561,9 @@ static int launch_fused(const Geometry& g, cplx<T>* X, int batch,
                X, g.P, g.cspec, bstride, TB, pitch, RtEng{p}, fp, mask);
     return BRI17_OK;
   }
+  if (MODE == kModeStiffness && g.use_ct3[0] &&
+      ct3_axis0_stiffness<T, DIM>(g.n[0], X, g.P, g.cspec, bstride, batch, fp, mask, st))
+    return BRI17_OK;
   const int n0 = g.n[0];
   const int pitch = n0 + 1;
   const size_t per_line = (size_t)(CMAX + 1) * pitch * sizeof(cplx<T>);

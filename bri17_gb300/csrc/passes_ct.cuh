@@ -352,6 +352,145 @@ void ct_set_smem_attrs_t(size_t max_smem) {
   cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Lengths 3 * 2^k on the twelve-element engine (CtEng3), FP32 and FP64:
+// 24..192 per strided axis, 48..384 on the last axis (rows of 24..192
+// complex points).  Same kernels and block shapes as the power-of-two
+// instances; the axis-0 pass takes the staged form (the registers form
+// holds 3 x 12 complex values per thread: 255 registers with spills in
+// FP32, against 84-118 staged).
+#define BRI17_CT3_CASES(X) X(24) X(48) X(96) X(192)
+
+template <typename T>
+bool ct3_rows_r2c(int m, const typename IoOf<T>::type* x, cplx<T>* X, int64_t nrows, int H,
+                  const cplx<T>* tw, BatchMask mask, cudaStream_t st) {
+  switch (m) {
+#define CASE(N)                                                                         \
+  case N: {                                                                             \
+    using Eng = CtEng3<N>;                                                              \
+    const int TT = Eng::kTT;                                                            \
+    const int rb = ct_rows_per_cta(TT, nrows, mask);                                    \
+    const int pitch = exchange_pitch(N, rb, (int)sizeof(cplx<T>), false, Eng::E);       \
+    const size_t smem = (3 * N + 1 + (size_t)rb * pitch) * sizeof(cplx<T>);             \
+    launch_pdl(rows_r2c_p2<T, Eng>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st, \
+               x, X, nrows, H, Eng{}, tw, rb, pitch, mask);                             \
+    return true;                                                                        \
+  }
+    BRI17_CT3_CASES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+template <typename T>
+bool ct3_rows_c2r(int m, const cplx<T>* X, typename IoOf<T>::type* x, int64_t nrows, int H,
+                  const cplx<T>* tw, BatchMask mask, cudaStream_t st) {
+  switch (m) {
+#define CASE(N)                                                                         \
+  case N: {                                                                             \
+    using Eng = CtEng3<N>;                                                              \
+    const int TT = Eng::kTT;                                                            \
+    const int rb = ct_rows_per_cta(TT, nrows, mask);                                    \
+    const int pitch = exchange_pitch(N, rb, (int)sizeof(cplx<T>), false, Eng::E);       \
+    const size_t smem = (3 * N + (size_t)rb * pitch) * sizeof(cplx<T>);                 \
+    launch_pdl(rows_c2r_p2<T, Eng>, (unsigned)((nrows + rb - 1) / rb), TT * rb, smem, st, \
+               X, x, nrows, H, Eng{}, tw, rb, pitch, mask);                             \
+    return true;                                                                        \
+  }
+    BRI17_CT3_CASES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+template <typename T, bool INV>
+bool ct3_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw,
+                  BatchMask mask, cudaStream_t st) {
+  switch (n) {
+#define CASE(N)                                                                          \
+  case N: {                                                                              \
+    using Eng = CtEng3<N>;                                                               \
+    const int TT = Eng::kTT;                                                             \
+    const int64_t nl = nouter * B;                                                       \
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, nl));    \
+    const int pitch = exchange_pitch(N, TB, (int)sizeof(cplx<T>), true, Eng::E);         \
+    const size_t smem = (N + (size_t)TB * pitch) * sizeof(cplx<T>);                      \
+    launch_pdl(axis_c2c_p2<T, INV, Eng>, (unsigned)((nl + TB - 1) / TB), TT * TB, smem, st, \
+               X, B, nl, TB, Eng{}, tw, pitch, mask);                                    \
+    return true;                                                                         \
+  }
+    BRI17_CT3_CASES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+template <typename T, int DIM>
+bool ct3_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t bstride,
+                         int batch, const FusedParams<T>& fp, BatchMask mask, cudaStream_t st) {
+  constexpr size_t csz = sizeof(cplx<T>);
+  switch (n0) {
+#define CASE(N)                                                                          \
+  case N: {                                                                              \
+    using Eng = CtEng3<N>;                                                               \
+    const int TT = Eng::kTT;                                                             \
+    const int TB = (int)std::max<int64_t>(1, std::min<int64_t>(kP2Threads / TT, P));     \
+    const int pitch = exchange_pitch(N, TB, (int)csz, true, Eng::E);                     \
+    const size_t smem =                                                                  \
+        (N + (size_t)TB * pitch + (size_t)DIM * TB * stash_pitch(N, TB, (int)csz)) * csz; \
+    dim3 grid((unsigned)((P + TB - 1) / TB), (unsigned)batch);                           \
+    launch_pdl(axis0_stiffness_staged<T, DIM, Eng>, grid, TT * TB, smem, st, X, P, cstride, \
+               bstride, TB, pitch, Eng{}, fp, mask);                                     \
+    return true;                                                                         \
+  }
+    BRI17_CT3_CASES(CASE)
+#undef CASE
+    default:
+      return false;
+  }
+}
+
+template <typename T>
+void ct3_set_smem_attrs_t(size_t max_smem) {
+#define CASE(N)                                                                          \
+  {                                                                                      \
+    using Eng = CtEng3<N>;                                                               \
+    cudaFuncSetAttribute(rows_r2c_p2<T, Eng>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)max_smem);                                                 \
+    cudaFuncSetAttribute(rows_c2r_p2<T, Eng>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)max_smem);                                                 \
+    cudaFuncSetAttribute(axis_c2c_p2<T, false, Eng>,                                     \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
+    cudaFuncSetAttribute(axis_c2c_p2<T, true, Eng>,                                      \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
+    cudaFuncSetAttribute(axis0_stiffness_staged<T, 2, Eng>,                              \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
+    cudaFuncSetAttribute(axis0_stiffness_staged<T, 3, Eng>,                              \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);    \
+  }
+  BRI17_CT3_CASES(CASE)
+#undef CASE
+  cudaGetLastError();
+}
+
+#define BRI17_CT3_INSTANTIATE(T)                                                             \
+  template bool ct3_rows_r2c<T>(int, const typename IoOf<T>::type*, cplx<T>*, int64_t, int, \
+                                const cplx<T>*, BatchMask, cudaStream_t);                   \
+  template bool ct3_rows_c2r<T>(int, const cplx<T>*, typename IoOf<T>::type*, int64_t, int, \
+                                const cplx<T>*, BatchMask, cudaStream_t);                   \
+  template bool ct3_axis_c2c<T, false>(int, cplx<T>*, int64_t, int64_t, const cplx<T>*,      \
+                                       BatchMask, cudaStream_t);                             \
+  template bool ct3_axis_c2c<T, true>(int, cplx<T>*, int64_t, int64_t, const cplx<T>*,       \
+                                      BatchMask, cudaStream_t);                              \
+  template bool ct3_axis0_stiffness<T, 2>(int, cplx<T>*, int64_t, int64_t, int64_t, int,    \
+                                          const FusedParams<T>&, BatchMask, cudaStream_t);    \
+  template bool ct3_axis0_stiffness<T, 3>(int, cplx<T>*, int64_t, int64_t, int64_t, int,    \
+                                          const FusedParams<T>&, BatchMask, cudaStream_t);    \
+  template void ct3_set_smem_attrs_t<T>(size_t);
+
 #define BRI17_CT_INSTANTIATE(T)                                                             \
   template bool ct_rows_r2c<T>(int, const typename IoOf<T>::type*, cplx<T>*, int64_t, int,  \
                                const cplx<T>*, BatchMask, cudaStream_t);                   \

@@ -75,6 +75,32 @@ struct CtEng {
   }
 };
 
+// Compile-time engine for lengths N = 3 * 2^k (fft8_ct.cuh PE3): twelve
+// elements per thread, per-stage twiddle tables (FP32 and FP64 only; the
+// float-pair passes are power-of-two only).
+template <int N>
+struct CtEng3 {
+  using P = PE3<N>;
+  static constexpr int E = P::kE;
+  static constexpr int kTT = P::T;
+  template <typename S>
+  static constexpr bool stage() {
+    return true;
+  }
+  __device__ __forceinline__ constexpr int n() const { return N; }
+  __device__ __forceinline__ constexpr int T() const { return P::T; }
+  template <typename S>
+  __device__ __forceinline__ void load_tw(cplx<S>* dst, const cplx<S>* __restrict__ src,
+                                          int count, int tws) const {
+    fftP_twiddles<S, P>(dst, src, tws, threadIdx.x, blockDim.x);
+  }
+  template <typename S, bool INV>
+  __device__ __forceinline__ void run(cplx<S> (&v)[E], cplx<S>* buf, int t,
+                                      const cplx<S>* __restrict__ tw, int tws) const {
+    fftP<S, P, INV>(v, buf, t, tw);
+  }
+};
+
 constexpr int kP2Threads = 256;
 constexpr int kP2FusedThreads = 128;
 
@@ -82,11 +108,15 @@ constexpr int kP2FusedThreads = 128;
 // allocator for: FP32 fits 32 registers (eight 256-thread CTAs, the whole
 // SM; 40 registers and six CTAs measured 79 -> 86 us at 256^3), float pairs
 // 64 (four); FP64 is bound by the FP64 pipe and takes what the compiler
-// picks.  The inverse row pass keeps the compiler's choice (FP32: 40
-// registers; capped at 32 it spills and measured 84 -> 89 us at 256^3).
-template <typename T>
+// picks.  With twelve elements per thread (lengths 3 * 2^k) 64 registers
+// (FP32) and 128 (FP64).  The inverse row pass keeps the compiler's choice
+// (FP32: 40 registers; capped at 32 it spills and measured 84 -> 89 us at
+// 256^3).
+template <typename T, int E = 8>
 struct RowCtas {
-  static constexpr int value = std::is_same<T, float>::value ? 8
+  static constexpr bool kF32 = std::is_same<T, float>::value;
+  static constexpr int value = E != 8 ? (kF32 ? 4 : 2)
+                               : kF32 ? 8
                                : std::is_same<T, df64>::value ? 4
                                                               : 1;
 };
@@ -124,7 +154,7 @@ __device__ __forceinline__ unsigned warp_lanes() {
 // Last axis, forward (n = 2m, m a power of two >= 8): rows of n reals ->
 // n/2+1 complex.  T = m/8 threads per row, RB rows per CTA.
 template <typename T, class Eng>
-__global__ void __launch_bounds__(kP2Threads, RowCtas<T>::value)
+__global__ void __launch_bounds__(kP2Threads, RowCtas<T, Eng::E>::value)
     rows_r2c_p2(const typename IoOf<T>::type* __restrict__ x, cplx<T>* __restrict__ X,
                 int64_t nrows, int H, Eng pm, const cplx<T>* __restrict__ tw_g, int RB,
                 int pitch, BatchMask mask) {
@@ -851,6 +881,22 @@ template <typename T, int DIM>
 bool ct_axis0_stiffness_staged(int n0, cplx<T>* X, int64_t P, int64_t cstride,
                                int64_t bstride, int batch, const FusedParams<T>& fp,
                                BatchMask mask, cudaStream_t st);
+// Lengths 3 * 2^k (passes_ct3_f32.cu / passes_ct3_f64.cu, FP32 and FP64
+// only): false, launching nothing, for lengths without an instance.
+template <typename T>
+bool ct3_rows_r2c(int m, const typename IoOf<T>::type* x, cplx<T>* X, int64_t nrows, int H,
+                  const cplx<T>* tw, BatchMask mask, cudaStream_t st);
+template <typename T>
+bool ct3_rows_c2r(int m, const cplx<T>* X, typename IoOf<T>::type* x, int64_t nrows, int H,
+                  const cplx<T>* tw, BatchMask mask, cudaStream_t st);
+template <typename T, bool INV>
+bool ct3_axis_c2c(int n, cplx<T>* X, int64_t B, int64_t nouter, const cplx<T>* tw,
+                  BatchMask mask, cudaStream_t st);
+template <typename T, int DIM>
+bool ct3_axis0_stiffness(int n0, cplx<T>* X, int64_t P, int64_t cstride, int64_t bstride,
+                         int batch, const FusedParams<T>& fp, BatchMask mask, cudaStream_t st);
+template <typename T>
+void ct3_set_smem_attrs_t(size_t max_smem);
 // TMA-staged forms (FP32, 3D; `keep` as KEEP above); false when the layout
 // does not meet the tensor-copy alignment rules.
 bool ct_axis0_stiffness_tma_f32(int n0, bool keep, cplx<float>* X, int64_t P, int64_t cstride,

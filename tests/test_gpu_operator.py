@@ -76,6 +76,11 @@ SHAPES = [
     ((1, 6, 10), (1.0, 1.0, 1.0), 1.0, 0.3),    # degenerate first axis
     ((8, 256, 64), (1.0, 2.0, 0.5), 1.0, 0.3),   # axis-1 lengths of the 16-element FP32 pass
     ((4, 512, 32), (1.0, 1.0, 1.0), 0.8, 0.2),
+    # lengths 3 * 2^k on the twelve-element engine: every axis and the rows
+    ((96, 96, 96), (1.0, 1.0, 1.0), 1.0, 0.3),
+    ((24, 192, 48), (0.5, 2.0, 1.0), 1.3, 0.35),
+    ((192, 24, 384), (2.0, 0.25, 4.0), 0.9, 0.2),
+    ((48, 3, 96), (1.0, 1.0, 1.0), 1.0, 0.3),
 ]
 
 
