@@ -101,6 +101,12 @@ int apply_stiffness_async(bri17_op* op, const void* u, void* f,
 // about four times its speed on GB300), else the handle's own operator.
 int prepare_accurate_residual(bri17_op* op);
 int apply_accurate_async(bri17_op* op, const double* u, double* f, cudaStream_t stream);
+// The same float-pair application with the material of one server slot:
+// `mat_df` (device) holds (s, mu) as two float pairs (hi, lo each), the
+// values the slot's FP64 residual would take from its (s, mu) doubles.
+// Needs prepare_accurate_residual to have enabled float pairs.
+int apply_accurate_mat_async(bri17_op* op, const double* u, double* f, const void* mat_df,
+                             cudaStream_t stream);
 
 // CG iterations on FP32 handles: whether the handle's stiffness pass can
 // sum p.Kp by Parseval (3D power-of-two grid with an even last axis, the

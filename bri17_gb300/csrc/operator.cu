@@ -20,7 +20,7 @@
 
 // The float-pair operator (defined with its C ABI below).
 static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
-                            cudaStream_t st);
+                            cudaStream_t st, const bri17gb::df64* mat = nullptr);
 
 namespace bri17gb {
 
@@ -1428,8 +1428,10 @@ extern "C" int bri17_modal_eigenstress_to_opposite_strain_host(const bri17_op* o
 
 // The five passes in float-pair arithmetic (3D, compile-time lengths
 // only).  `form` selects the axis-0 pass: 2 TMA-staged, else staged.
+// `mat` (optional, device): the (s, mu) pair of this application as float
+// pairs, overriding the handle's material (the server's slots).
 static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
-                            cudaStream_t st) {
+                            cudaStream_t st, const df64* mat) {
   if (env_fused_form() >= 0) form = env_fused_form();
   const Geometry& g = op->g;
   const int dim = g.dim;
@@ -1453,6 +1455,7 @@ static int run_stiffness_df(bri17_op* op, const double* u, double* f, int form,
   if (ok) {
     PassScope ps(op, 2, st);
     FusedParams<df64> fp = fused_params<df64>(op, tab, kModeStiffness);
+    fp.mat = mat;
     const int64_t bstride = (int64_t)dim * g.cspec;
     bool done = false;
     if (form == 2 && dim == 3)
@@ -1610,6 +1613,17 @@ int bri17gb::prepare_accurate_residual(bri17_op* op) {
   if (rc != BRI17_OK) return rc;
   op->residual_df = true;
   return BRI17_OK;
+}
+
+int bri17gb::apply_accurate_mat_async(bri17_op* op, const double* u, double* f,
+                                      const void* mat_df, cudaStream_t st) {
+  if (!op->residual_df) {
+    set_error("internal: float-pair residual not prepared");
+    return BRI17_ERR_UNSUPPORTED_SIZE;
+  }
+  const int rc = ensure_spectrum(op, op->g.dim);
+  if (rc != BRI17_OK) return rc;
+  return ::run_stiffness_df(op, u, f, op->fused_form_df, st, static_cast<const df64*>(mat_df));
 }
 
 int bri17gb::apply_accurate_async(bri17_op* op, const double* u, double* f, cudaStream_t st) {

@@ -69,6 +69,7 @@ struct Request {
   double bb = 0, rel = 1, nr = 0;
   double mat64[2] = {0, 0};  // upload sources (live until the copies ran)
   float mat32[2] = {0, 0};
+  float matdf[4] = {0, 0, 0, 0};  // (s, mu) as float pairs (hi, lo)
   int status = BRI17_OK;
   bool cancel = false;
 };
@@ -89,6 +90,7 @@ struct Bucket {
   float *d = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
   float* mat32 = nullptr;
   double* mat64 = nullptr;
+  float* matdf = nullptr;  // per slot (s, mu) as float pairs, for float-pair residuals
   void* spec32 = nullptr;
   CgState* st = nullptr;
   CgState* st_host = nullptr;
@@ -379,7 +381,7 @@ void free_bucket(Bucket* B) {
   bri17_op_destroy(B->op32);
   bri17_op_destroy(B->op64);
   void* ps[] = {B->b, B->x, B->r, B->q64, B->tau, B->d, B->r32, B->p32, B->q32,
-                B->mat32, B->mat64, B->spec32, B->st, B->partials};
+                B->mat32, B->mat64, B->matdf, B->spec32, B->st, B->partials};
   for (void* p : ps) cudaFree(p);
   cudaFreeHost(B->st_host);
   if (B->stream) cudaStreamDestroy(B->stream);
@@ -444,6 +446,13 @@ int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
   if (rc != BRI17_OK) return fail(rc);
   rc = ensure_spectrum(B->op64, 6);
   if (rc != BRI17_OK) return fail(rc);
+  // Float-pair tables for the slots' FP64 residuals where the grid has
+  // float-pair instances; without them (or if building them fails) the
+  // residuals stay on the FP64 pipe.
+  if (prepare_accurate_residual(B->op64) != BRI17_OK) {
+    B->op64->residual_df = false;
+    cudaGetLastError();
+  }
   const int64_t n = B->n, Sn = S * n;
   const int64_t cspec = B->op32->g.cspec;
   // An injected failure takes the place of work buffer number inject_at.
@@ -467,6 +476,7 @@ int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
   ALLOC(B->q32, Sn * 4);
   ALLOC(B->mat32, S * 2 * 4);
   ALLOC(B->mat64, S * 2 * 8);
+  ALLOC(B->matdf, S * 4 * 4);
   ALLOC(B->spec32, (int64_t)S * 3 * cspec * 8);
   ALLOC(B->st, S * sizeof(CgState));
   ALLOC(B->partials, (int64_t)S * kRedMaxBlocks * 8);
@@ -477,6 +487,7 @@ int make_bucket(bri17_server* srv, const Request* q, Bucket** out) {
   if (cudaMemset(B->st, 0, S * sizeof(CgState)) != cudaSuccess ||
       cudaMemset(B->mat32, 0, S * 2 * 4) != cudaSuccess ||
       cudaMemset(B->mat64, 0, S * 2 * 8) != cudaSuccess ||
+      cudaMemset(B->matdf, 0, S * 4 * 4) != cudaSuccess ||
       cudaMemset(B->p32, 0, Sn * 4) != cudaSuccess)
     return fail(cuda_fail(cudaErrorUnknown, "cudaMemset(bucket)"));
   // With size priorities on, smaller geometries get higher stream priority:
@@ -531,8 +542,12 @@ int enqueue_residual(Bucket* B, int z, bool x_is_zero) {
     dim3 gm(std::min(red_blocks(B->size), kRedMaxBlocks / 3), 3);
     ks_comp_mean<<<gm, kRedThreads, 0, s>>>(xz, B->size, st, parts);
     ks_sub_mean<<<dim3(g1(B->size), 3), 256, 0, s>>>(xz, B->size, st);
-    int rc = apply_stiffness_batched_async(B->op64, 1, xz, B->q64 + z * n, B->op64->spec,
-                                           B->mat64 + 2 * z, s);
+    // FP64-accurate K x in float pairs where the grid has them (64^3 and
+    // larger power-of-two sides), else on the FP64 pipe.
+    int rc = B->op64->residual_df
+                 ? apply_accurate_mat_async(B->op64, xz, B->q64 + z * n, B->matdf + 4 * z, s)
+                 : apply_stiffness_batched_async(B->op64, 1, xz, B->q64 + z * n,
+                                                 B->op64->spec, B->mat64 + 2 * z, s);
     if (rc != BRI17_OK) return rc;
     ks_residual<<<g1(n), 256, 0, s>>>(rz, bz, B->q64 + z * n, n);
   }
@@ -583,6 +598,15 @@ int admit(bri17_server* srv, Bucket* B, int z, Request* q) {
                           s));
   SRV_TRY(cudaMemcpyAsync(B->mat32 + 2 * z, q->mat32, sizeof(q->mat32), cudaMemcpyHostToDevice,
                           s));
+  if (B->op64->residual_df) {
+    const df64 sdf(q->mat64[0]), mdf(q->mat64[1]);
+    q->matdf[0] = sdf.hi;
+    q->matdf[1] = sdf.lo;
+    q->matdf[2] = mdf.hi;
+    q->matdf[3] = mdf.lo;
+    SRV_TRY(cudaMemcpyAsync(B->matdf + 4 * z, q->matdf, sizeof(q->matdf),
+                            cudaMemcpyHostToDevice, s));
+  }
   int rc = eigenstress_rhs_batched_async(B->op64, 1, B->tau, B->b + z * n, B->op64->spec, s);
   if (rc != BRI17_OK) return rc;
   SRV_TRY(cudaMemsetAsync(B->x + z * n, 0, n * 8, s));
