@@ -32,7 +32,11 @@ def _lib_pitch():
 def _stages(n, E):
     """Radices of the engines' stages: E = 8 takes 8s and ends with 4 x 4
     (log2 n = 1 mod 3) or one 4 (2 mod 3); E = 16 takes 16s and ends with the
-    remaining power of two."""
+    remaining power of two; E = 12 (n = 3 * 2^k) takes 4s, one 2 when k is
+    odd, and the 3 last."""
+    if E == 12:
+        k = (n // 3).bit_length() - 1
+        return n // 12, [4] * (k // 2) + [2] * (k % 2) + [3]
     e = n.bit_length() - 1
     if E == 8:
         a, b = divmod(e, 3)
@@ -94,6 +98,12 @@ CASES = [(n, lines, cs, lf, 8)
          for lf in (True, False)
          if (n // 8) * lines <= 512]
 CASES += [(n, lines, 8, True, 16) for n in (256, 512) for lines in (2, 4, 8, 16)]
+CASES += [(n, lines, cs, lf, 12)
+          for n in (24, 48, 96, 192)
+          for lines in (1, 4, 16)
+          for cs in (8, 16)
+          for lf in (True, False)
+          if (n // 12) * lines <= 256]
 
 
 @pytest.mark.parametrize("n,lines,csize,lines_fastest,E", CASES)
