@@ -207,25 +207,48 @@ __global__ void __launch_bounds__(kP2Threads, RowCtas<T, Eng::E>::value)
   }
   cplx<T>* out = X + row * H;
   // X_k = (A + W D) / 2 with A = Z_k + conj(Z_{m-k}), D = -i (Z_k -
-  // conj(Z_{m-k})); the 1/2 lives in the twh table and one fused
+  // conj(Z_{m-k})), W = W_n^k; the 1/2 lives in the twh table and one fused
   // multiply-add per part.
+  if constexpr (kShfl) {
+    // A_{m-k} = conj(A_k), D_{m-k} = conj(D_k) and W^{m-k} = -conj(W^k), so
+    // X_{m-k} = conj(A_k/2 - W D_k/2): each thread forms both outputs of
+    // its pairs k < m/2 (for k = 0 the pair is X_0 and X_m), half the
+    // arithmetic and half the shuffles of one output per element.
+    constexpr int EH = Eng::E / 2;
 #pragma unroll
-  for (int q = 0; q < Eng::E; q++) {
-    const int k = t + TT * q;
-    const cplx<T> zk = v[q];
-    cplx<T> zm;
-    if constexpr (kShfl) {
+    for (int q = 0; q < EH; q++) {
+      const int k = t + TT * q;
       const cplx<T> o = shfl_cplx<T>(lanes, v[Eng::E - 1 - q], src);
-      zm = t == 0 ? v[(Eng::E - q) % Eng::E] : o;
-    } else {
-      zm = buf[pad16((m - k) & (m - 1))];
+      const cplx<T> zk = v[q];
+      const cplx<T> zm = t == 0 ? v[(Eng::E - q) % Eng::E] : o;
+      const cplx<T> A = mk<T>(zk.x + zm.x, zk.y - zm.y);
+      const cplx<T> D = mk<T>(zk.y + zm.y, zm.x - zk.x);
+      const cplx<T> WD = cmul<T>(twh[k], D);
+      if (valid) {
+        out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
+        out[m - k] = mk<T>(fma(T(0.5), A.x, -WD.x), -fma(T(0.5), A.y, -WD.y));
+      }
     }
-    const cplx<T> A = mk<T>(zk.x + zm.x, zk.y - zm.y);
-    const cplx<T> D = mk<T>(zk.y + zm.y, zm.x - zk.x);
-    const cplx<T> WD = cmul<T>(twh[k], D);
-    if (valid) out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
+    if (valid && t == 0) {  // k = m/2, its own mirror
+      const cplx<T> z = v[EH];
+      const cplx<T> A = mk<T>(z.x + z.x, z.y - z.y);
+      const cplx<T> D = mk<T>(z.y + z.y, z.x - z.x);
+      const cplx<T> WD = cmul<T>(twh[m / 2], D);
+      out[m / 2] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < Eng::E; q++) {
+      const int k = t + TT * q;
+      const cplx<T> zk = v[q];
+      const cplx<T> zm = buf[pad16((m - k) & (m - 1))];
+      const cplx<T> A = mk<T>(zk.x + zm.x, zk.y - zm.y);
+      const cplx<T> D = mk<T>(zk.y + zm.y, zm.x - zk.x);
+      const cplx<T> WD = cmul<T>(twh[k], D);
+      if (valid) out[k] = mk<T>(fma(T(0.5), A.x, WD.x), fma(T(0.5), A.y, WD.y));
+    }
+    if (valid && t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
   }
-  if (valid && t == 0) out[m] = mk<T>(v[0].x - v[0].y, T(0));
 }
 
 // Last axis, inverse: n/2+1 complex -> n reals (unnormalised).
@@ -266,8 +289,15 @@ __global__ void __launch_bounds__(kP2Threads)
     const cplx<T> wm = (valid && t == 0) ? in[m] : zero;
     const unsigned lanes = warp_lanes();
     const int src = mirror_lane<Eng::kTT>(t);
+    // Z_k = A + i conj(W^k) D with A = X_k + conj(X_{m-k}), D = X_k -
+    // conj(X_{m-k}); as in the forward pass Z_{m-k} = conj(A - i conj(W^k)
+    // D), so each thread forms the pair of its k < m/2 and hands Z_{m-k} to
+    // the mirror thread, which holds it as element E-1-q (thread 0 holds its
+    // own mirrors, Z_{m-k} as element E-q, and Z_{m/2}).
+    constexpr int EH = Eng::E / 2;
+    cplx<T> zmir[EH];
 #pragma unroll
-    for (int q = 0; q < Eng::E; q++) {
+    for (int q = 0; q < EH; q++) {
       const int k = t + TT * q;
       const cplx<T> o = shfl_cplx<T>(lanes, w[Eng::E - 1 - q], src);
       const cplx<T> xk = w[q];
@@ -276,6 +306,23 @@ __global__ void __launch_bounds__(kP2Threads)
       const cplx<T> D = mk<T>(xk.x - xm.x, xk.y + xm.y);
       const cplx<T> Bv = cmulc<T>(D, tw[k]);
       v[q] = mk<T>(A.x - Bv.y, A.y + Bv.x);
+      zmir[q] = mk<T>(A.x + Bv.y, Bv.x - A.y);
+    }
+    cplx<T> zhalf = zero;
+    if (t == 0) {  // k = m/2, its own mirror
+      const cplx<T> x = w[EH];
+      const cplx<T> A = mk<T>(x.x + x.x, x.y - x.y);
+      const cplx<T> D = mk<T>(x.x - x.x, x.y + x.y);
+      const cplx<T> Bv = cmulc<T>(D, tw[m / 2]);
+      zhalf = mk<T>(A.x - Bv.y, A.y + Bv.x);
+    }
+#pragma unroll
+    for (int q = 0; q < EH; q++) {
+      const cplx<T> r = shfl_cplx<T>(lanes, zmir[q], src);
+      // Element E-1-q: the mirror's Z_{m-k}; for thread 0 its own Z_{m/2}
+      // (q = EH-1) or the mirror of its element E-1-q.
+      const int j = Eng::E - 1 - q;
+      v[j] = t != 0 ? r : (j == EH ? zhalf : zmir[(Eng::E - j) % EH]);
     }
   } else {
 #pragma unroll
