@@ -131,10 +131,11 @@ int bri17_op_set_material(bri17_op* op, double mu, double nu);
  * counterpart): 0 register-resident, 1 shared-memory staged, 2 TMA-staged
  * (tensor copies of whole tiles; FP32, 3D, even shape[1]), 3 TMA-staged with
  * the spectra kept in registers between the transforms (float-pair
- * handles: 1 or 2, other values select 1).  FP32 handles
- * pick the fastest by timing at creation.  A form that does not apply to the
- * handle's grid falls back to the next applicable one at launch.  Results
- * agree between forms to rounding.
+ * handles: 1 or 2, other values select 1).  FP32 handles with a
+ * power-of-two first axis pick the fastest by timing at creation; a first
+ * axis of length 3 * 2^k (24..192) always takes the staged form.  A form
+ * that does not apply to the handle's grid falls back to the next
+ * applicable one at launch.  Results agree between forms to rounding.
  */
 int bri17_op_fused_form(const bri17_op* op, int* form);
 int bri17_op_set_fused_form(bri17_op* op, int form);
