@@ -93,6 +93,21 @@ __global__ void __launch_bounds__(kRedThreads)
     st->aux = tot;
 }
 
+// aux = |b - kx|^2 (the true residual's square norm, from K x in kx).
+__global__ void __launch_bounds__(kRedThreads)
+    k_resnorm(const double* __restrict__ b, const double* __restrict__ kx, int64_t n,
+              CgState* st, double* partials) {
+  double v = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = b[i] - kx[i];
+    v += d * d;
+  }
+  double tot;
+  if (last_block_total(v, partials, &st->counter, gridDim.x, &tot) && threadIdx.x == 0)
+    st->aux = tot;
+}
+
 // Per-component means of a dim x size field (grid.y = component).
 __global__ void __launch_bounds__(kRedThreads)
     k_comp_mean(const double* __restrict__ a, int64_t size, CgState* st,
@@ -211,6 +226,14 @@ __global__ void __launch_bounds__(kRedThreads)
 // FP64 one (aux = its squared norm); keep the search direction, resume.
 // At least one more chunk runs even when the replaced residual already meets
 // the FP32 threshold, so every update changes the iterate.
+// The plain solver's resumption after a true-residual check: same CG, a new
+// pause threshold.
+__global__ void k_plain_resume(CgState* st, double thresh) {
+  st->thresh = thresh;
+  st->pause = 0;
+  st->active = (st->rr > thresh && isfinite(st->rr)) ? 1 : 0;
+}
+
 __global__ void k_reliable_resume(CgState* st, double thresh) {
   st->rr = st->aux;
   st->thresh = thresh;
@@ -227,6 +250,7 @@ struct CgWork {
   double* x;        // FP64 iterate (work copy)
   double* r;        // FP64 residual
   double* p;        // FP64 search direction (plain mode)
+  double* xbest;    // plain mode: the iterate with the smallest true residual seen
   double* q;        // FP64 K p / K x
   float* d32;       // FP32 inner iterate (mixed mode)
   float* r32;
@@ -253,6 +277,7 @@ static void cg_free(void* p) {
   cudaFree(w->x);
   cudaFree(w->r);
   cudaFree(w->p);
+  cudaFree(w->xbest);
   cudaFree(w->q);
   cudaFree(w->d32);
   cudaFree(w->r32);
@@ -289,6 +314,7 @@ static int ensure_work(bri17_op* op, bool mixed, CgWork** out) {
   if (!mixed && !w->plain_ready) {
     if (op->precision == BRI17_F64) {
       BRI17_CUDA_TRY(cudaMalloc(&w->p, n * sizeof(double)));
+      BRI17_CUDA_TRY(cudaMalloc(&w->xbest, n * sizeof(double)));
     } else {
       BRI17_CUDA_TRY(cudaMalloc(&w->d32, n * sizeof(float)));
       BRI17_CUDA_TRY(cudaMalloc(&w->r32, n * sizeof(float)));
@@ -452,10 +478,89 @@ static int solve_plain64(bri17_op* op, const double* b, double* x, double tol,
   // aux must hold b.b for k_start's threshold.
   k_dot<double><<<rb, kRedThreads, 0, s>>>(b, b, n, w->st, w->partials);
   k_start<double><<<rb, kRedThreads, 0, s>>>(w->r, w->p, n, w->st, w->partials, tol * tol);
+  // The recursive residual can stop tracking the true one once the true one
+  // reaches what FP64 resolves: below that the recursion may stall above a
+  // tolerance that cannot be met, or run on while the iterate drifts and
+  // even diverges.  So the true residual |b - K x| is computed (K x into q,
+  // which each iteration overwrites anyway) whenever the recursive one has
+  // dropped 100x since the last check, and at least every kCheck
+  // iterations; the iterate with the smallest true residual is kept.  The
+  // solve succeeds when the true residual meets tol, and stops as
+  // stagnated, returning the kept iterate, when the recursive residual has
+  // met tol but the true one has not, when the true residual has not halved
+  // over kStallChecks checks while the recursive one sits 10x or more below
+  // it (or it has grown past 4x the last halving), over 2 kStallChecks
+  // checks in any case, or when it has grown past 10x its smallest.
+  constexpr int kCheck = 256;
+  constexpr int kStallChecks = 4;
   int iters = 0;
-  int status = run_cg<double>(op, w, w->x, w->r, w->p, w->q, &w->graph64,
-                              &w->epoch64, maxit, &iters);
+  int status = BRI17_ERR_NOT_CONVERGED;
+  double best = INFINITY, prog = INFINITY;
+  int since_prog = 0;
+  bool have_best = false;
+  rc = read_state(w);
+  if (rc != BRI17_OK) return rc;
+  const double thresh_tol = tol * tol * bb;
+  const bool start_active = w->st_host->active != 0;
+  if (!start_active)  // converged at the start, or a breakdown
+    status = w->st_host->flag != BRI17_OK ? w->st_host->flag : BRI17_OK;
+  for (int budget = 0; start_active;) {
+    k_plain_resume<<<1, 1, 0, s>>>(w->st, std::max(thresh_tol, 1e-4 * w->st_host->rr));
+    budget = (int)std::min<int64_t>(maxit, (int64_t)iters + kCheck);
+    // BRI17_OK here: paused at the threshold (a 100x drop, or tol).
+    status = run_cg<double>(op, w, w->x, w->r, w->p, w->q, &w->graph64, &w->epoch64, budget,
+                            &iters);
+    if ((status != BRI17_OK && status != BRI17_ERR_NOT_CONVERGED) ||
+        (status == BRI17_ERR_NOT_CONVERGED && iters >= maxit))
+      break;
+    rc = apply_stiffness_async(op, w->x, w->q, s);
+    if (rc != BRI17_OK) return rc;
+    k_resnorm<<<rb, kRedThreads, 0, s>>>(b, w->q, n, w->st, w->partials);
+    rc = read_state(w);
+    if (rc != BRI17_OK) return rc;
+    const double rt = w->st_host->aux, rr = w->st_host->rr;
+    if (!isfinite(rt)) {
+      status = BRI17_ERR_BREAKDOWN;
+      break;
+    }
+    if (rt <= thresh_tol) {
+      status = BRI17_OK;
+      have_best = false;  // the current iterate is the answer
+      break;
+    }
+    if (rt < best) {
+      best = rt;
+      have_best = true;
+      BRI17_CUDA_TRY(cudaMemcpyAsync(w->xbest, w->x, n * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, s));
+    }
+    if (rr <= thresh_tol) {  // the recursion met tol, the true residual did not
+      status = BRI17_ERR_STAGNATED;
+      break;
+    }
+    if (rt < 0.25 * prog) {
+      prog = rt;
+      since_prog = 0;
+    } else if (++since_prog >= kStallChecks &&
+               (rr < 0.01 * rt || rt > 16.0 * prog || since_prog >= 2 * kStallChecks)) {
+      status = BRI17_ERR_STAGNATED;
+      break;
+    }
+    if (rt > 100.0 * best) {
+      status = BRI17_ERR_STAGNATED;
+      break;
+    }
+    if (iters >= maxit) {
+      status = BRI17_ERR_NOT_CONVERGED;
+      break;
+    }
+  }
+  if (status == BRI17_ERR_STAGNATED && have_best)
+    BRI17_CUDA_TRY(cudaMemcpyAsync(w->x, w->xbest, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   s));
   if (status == BRI17_ERR_CUDA || status == BRI17_ERR_OUT_OF_MEMORY) return status;
+  if (status == BRI17_ERR_STAGNATED)
+    set_error("the true CG residual stopped decreasing above tol (FP64 cannot resolve tol)");
   project_mean(op, w, w->x);
   rc = residual64(op, w, b);
   if (rc != BRI17_OK) return rc;
