@@ -355,8 +355,11 @@ typedef struct bri17_cg_info {
  * from the FP64 operator) whenever the grid has float-pair instances, with
  * float pairs on the handle or not; BRI17_MIXED_RESIDUAL=f64 in the
  * environment keeps them on the FP64 pipe.  The plain solver on an FP64
- * handle stays on the FP64 pipe unless float pairs are on.  Synchronises
- * `stream` (the stopping test reads the residual).
+ * handle stays on the FP64 pipe unless float pairs are on; it recomputes
+ * the true residual at every 100x drop of the recursive one (and at least
+ * every 256 iterations) and, when that stops decreasing above tol, returns
+ * BRI17_ERR_STAGNATED with the iterate of smallest true residual in x_dev.
+ * Synchronises `stream` (the stopping test reads the residual).
  */
 int bri17_cg_solve(bri17_op* op, const double* b_dev, double* x_dev,
                    double tol, int max_iterations, int mode,
