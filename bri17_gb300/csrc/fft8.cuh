@@ -48,6 +48,13 @@ inline bool make_plan8(int n, Plan8* p) {
 
 // Shared-memory position of element p of a line: one pad slot per 16.
 __device__ __forceinline__ int pad16(int p) { return p + (p >> 4); }
+// Position of element p in an exchange buffer: the line's own padded buffer
+// (BS = 0), or every BS-th entry (BS > 0: the line interleaved with BS - 1
+// others, as in a staged tile laid out [p][line]).
+template <int BS>
+__device__ __forceinline__ int xpos(int p) {
+  return BS > 0 ? p * BS : pad16(p);
+}
 // Line pitch (complex elements, odd so consecutive lines use distinct banks).
 __host__ __device__ __forceinline__ int pitch8(int n) { return n + n / 16 + 1; }
 
@@ -71,8 +78,9 @@ __host__ __device__ __forceinline__ int stash_pitch(int n, int TB, int csize) {
   return (n + M - 1) / M * M + (s % M == 0 ? M / 2 + 1 : s % M);
 }
 
-// One radix-R stage with E elements per thread (E/R butterflies per thread).
-template <typename T, int R, int E, bool INV>
+// One radix-R stage with E elements per thread (E/R butterflies per thread);
+// BS as in xpos.
+template <typename T, int R, int E, bool INV, int BS = 0>
 __device__ __forceinline__ void stageE(cplx<T> (&v)[E], cplx<T>* buf, int t, int TT,
                                        int Ns, int n, const cplx<T>* __restrict__ tw,
                                        int tws, bool last) {
@@ -96,7 +104,7 @@ __device__ __forceinline__ void stageE(cplx<T> (&v)[E], cplx<T>* buf, int t, int
     } else {
       const int d = (j - jm) * R + jm;
 #pragma unroll
-      for (int r = 0; r < R; r++) buf[pad16(d + r * Ns)] = a[r];
+      for (int r = 0; r < R; r++) buf[xpos<BS>(d + r * Ns)] = a[r];
     }
   }
 }

@@ -170,26 +170,28 @@ __device__ __forceinline__ void fftE_ct(cplx<T> (&v)[E], cplx<T>* buf, int t,
   fftP<T, PE<N, E>, INV>(v, buf, t, stw);
 }
 
-// The same transform reading the natural table `tw` with stride tws.
-template <typename T, int N, int E, bool INV, int S, int NS>
+// The same transform reading the natural table `tw` with stride tws; the
+// exchanges go through `buf` at xpos<BS> (BS = 0: the line's own padded
+// buffer).
+template <typename T, int N, int E, bool INV, int S, int NS, int BS = 0>
 __device__ __forceinline__ void fftE_ct_stage_nat(cplx<T> (&v)[E], cplx<T>* buf, int t,
                                                   const cplx<T>* __restrict__ tw, int tws) {
   constexpr int R = PE<N, E>::radix(S);
   constexpr bool LAST = S == PE<N, E>::NST - 1;
-  stageE<T, R, E, INV>(v, buf, t, PE<N, E>::T, NS, N, tw, tws, LAST);
+  stageE<T, R, E, INV, BS>(v, buf, t, PE<N, E>::T, NS, N, tw, tws, LAST);
   if constexpr (!LAST) {
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < E; q++) v[q] = buf[pad16(t + PE<N, E>::T * q)];
+    for (int q = 0; q < E; q++) v[q] = buf[xpos<BS>(t + PE<N, E>::T * q)];
     __syncthreads();
-    fftE_ct_stage_nat<T, N, E, INV, S + 1, NS * R>(v, buf, t, tw, tws);
+    fftE_ct_stage_nat<T, N, E, INV, S + 1, NS * R, BS>(v, buf, t, tw, tws);
   }
 }
 
-template <typename T, int N, int E, bool INV>
+template <typename T, int N, int E, bool INV, int BS = 0>
 __device__ __forceinline__ void fftE_ct_nat(cplx<T> (&v)[E], cplx<T>* buf, int t,
                                             const cplx<T>* __restrict__ tw, int tws) {
-  fftE_ct_stage_nat<T, N, E, INV, 0, 1>(v, buf, t, tw, tws);
+  fftE_ct_stage_nat<T, N, E, INV, 0, 1, BS>(v, buf, t, tw, tws);
 }
 
 

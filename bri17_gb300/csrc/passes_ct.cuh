@@ -225,14 +225,27 @@ int tma_pitch() {
   return exchange_pitch(N, tma_lines<T>(N), (int)sizeof(cplx<T>), true);
 }
 
+// Float pairs exchange inside the tile (axis0_stiffness_tma's XS) when a
+// tile row is 128 bytes, TB = 8 lines of 16 bytes (n0 = 64, 128): 0
+// otherwise, and for FP32, whose staged compute keeps its exchange buffer.
+template <typename T, int N>
+constexpr int tma_xs() {
+  return std::is_same<T, df64>::value && tma_lines<T>(N) * (int)sizeof(cplx<T>) == 128
+             ? tma_lines<T>(N)
+             : 0;
+}
+
 // Shared memory the p.Kp reduction of the PQ instance adds after the
 // mbarrier: 8 warp sums and the last-CTA flag.
 constexpr size_t kTmaPqSmem = 80;
 
+// Dynamic shared memory of the staged-compute instance (XS = tma_xs) or,
+// with xs = 0 forced, of the instances with an exchange buffer.
 template <typename T, int N>
-size_t tma_smem_bytes() {
+size_t tma_smem_bytes(bool with_exchange = tma_xs<T, N>() == 0) {
   constexpr int TB = tma_lines<T>(N);
-  return ((size_t)3 * N * TB + (size_t)TB * tma_pitch<T, N>() + N) * sizeof(cplx<T>) + 16;
+  const size_t exch = with_exchange ? (size_t)TB * tma_pitch<T, N>() : 0;
+  return ((size_t)3 * N * TB + exch + N) * sizeof(cplx<T>) + 16;
 }
 
 // WITH_KEEP = false compiles only the staged-compute variant (keep is then
@@ -267,7 +280,7 @@ bool ct_axis0_stiffness_tma(int n0, bool keep, cplx<T>* X, int64_t P, int64_t cs
     if constexpr (WITH_KEEP) {                                                           \
       if (keep) {                                                                        \
         launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, true>, grid, TT * TB,        \
-                   tma_smem_bytes<T, N>(), st, map, P, TB, tma_pitch<T, N>(),            \
+                   tma_smem_bytes<T, N>(true), st, map, P, TB, tma_pitch<T, N>(),        \
                    CtEng<N, E>{}, fp, mask);                                             \
         launched = true;                                                                 \
       }                                                                                  \
@@ -276,15 +289,15 @@ bool ct_axis0_stiffness_tma(int n0, bool keep, cplx<T>* X, int64_t P, int64_t cs
       if (!launched && fp.cg) {                                                          \
         if (batch != 1) return false;                                                    \
         launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, false, true>, grid, TT * TB, \
-                   tma_smem_bytes<T, N>() + kTmaPqSmem, st, map, P, TB,                  \
+                   tma_smem_bytes<T, N>(true) + kTmaPqSmem, st, map, P, TB,              \
                    tma_pitch<T, N>(), CtEng<N, E>{}, fp, mask);                          \
         launched = true;                                                                 \
       }                                                                                  \
     }                                                                                    \
     if (!launched)                                                                       \
-      launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, false>, grid, TT * TB,         \
-                 tma_smem_bytes<T, N>(), st, map, P, TB, tma_pitch<T, N>(), CtEng<N, E>{}, \
-                 fp, mask);                                                              \
+      launch_pdl(axis0_stiffness_tma<T, DIM, CtEng<N, E>, false, false, tma_xs<T, N>()>, \
+                 grid, TT * TB, tma_smem_bytes<T, N>(), st, map, P, TB, tma_pitch<T, N>(), \
+                 CtEng<N, E>{}, fp, mask);                                               \
     return true;                                                                         \
     }                                                                                 \
   }
@@ -299,17 +312,17 @@ template <typename T, bool WITH_KEEP = true>
 void ct_set_smem_attrs_tma(size_t max_smem) {
 #define CASE(N)                                                                          \
   if constexpr (ct_has<T>(N)) {                                                          \
-    cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, false>,                  \
+    cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, false, false, tma_xs<T, N>()>, \
                          cudaFuncAttributeMaxDynamicSharedMemorySize,                    \
                          (int)std::min(max_smem, tma_smem_bytes<T, N>()));               \
     if constexpr (WITH_KEEP)                                                             \
       cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, true>,                 \
                            cudaFuncAttributeMaxDynamicSharedMemorySize,                  \
-                           (int)std::min(max_smem, tma_smem_bytes<T, N>()));             \
+                           (int)std::min(max_smem, tma_smem_bytes<T, N>(true)));         \
     if constexpr (std::is_same<T, float>::value)                                         \
       cudaFuncSetAttribute(axis0_stiffness_tma<T, 3, CtEng<N, 8>, false, true>,          \
                            cudaFuncAttributeMaxDynamicSharedMemorySize,                  \
-                           (int)std::min(max_smem, tma_smem_bytes<T, N>() + kTmaPqSmem)); \
+                           (int)std::min(max_smem, tma_smem_bytes<T, N>(true) + kTmaPqSmem)); \
   }
   CASE(16) CASE(32) CASE(64) CASE(128) CASE(256) CASE(512) CASE(1024)
 #undef CASE

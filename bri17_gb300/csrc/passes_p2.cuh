@@ -73,6 +73,17 @@ struct CtEng {
     else
       fftE_ct_nat<S, N, EE, INV>(v, buf, t, tw, tws);
   }
+  // The same transform with the exchanges at every BS-th entry of `buf`
+  // (the line's column of a tile laid out [element][BS lines]); natural
+  // twiddle table only.  The first exchange writes `buf` without a barrier
+  // before it: the caller makes sure every thread of the line has read what
+  // it needs from there.
+  template <typename S, bool INV, int BS>
+  __device__ __forceinline__ void run_strided(cplx<S> (&v)[EE], cplx<S>* buf, int t,
+                                              const cplx<S>* __restrict__ tw, int tws) const {
+    static_assert(!stage<S>() && BS > 0, "strided exchanges read the natural table");
+    fftE_ct_nat<S, N, EE, INV, BS>(v, buf, t, tw, tws);
+  }
 };
 
 // Compile-time engine for lengths N = 3 * 2^k (fft8_ct.cuh PE3): twelve
@@ -714,18 +725,30 @@ static __device__ unsigned long long g_tma_wait_limit_ns = kWaitLimitNs;
 // registers at a time); true keeps all DIM components in registers from the
 // forward transforms through K(k) u(k) to the inverse ones (fewer
 // shared-memory round trips, more registers).
-template <typename T, int DIM, class Eng, bool KEEP, bool PQ = false>
+//
+// XS > 0 (float pairs, TB = XS lines of 128 bytes per tile row): a
+// component's transforms exchange through the component's own slot of the
+// tile -- element p of line tb at row p, column tb -- instead of a separate
+// exchange buffer.  The slot's values are in registers while it is
+// transformed, so it is free; one barrier after the loads keeps the first
+// exchange from overwriting values other threads of the line have not
+// loaded yet.  A warp's lanes cover the TB lines of four rows, so each
+// access takes the four wavefronts its 512 bytes need, and the CTA's shared
+// memory shrinks by the exchange buffer (128^3: 69 -> 52 KB, four resident
+// CTAs per SM instead of three).
+template <typename T, int DIM, class Eng, bool KEEP, bool PQ = false, int XS = 0>
 __global__ void __launch_bounds__(256)
     axis0_stiffness_tma(const __grid_constant__ CUtensorMap map, int64_t P, int TB, int pitch,
                         Eng p0, FusedParams<T> fp, BatchMask mask) {
   static_assert(DIM == 3, "three-dimensional grids only");
+  static_assert(XS == 0 || (!KEEP && !PQ), "in-tile exchanges: staged compute only");
   extern __shared__ __align__(128) unsigned char smem_tma[];
   constexpr int kPer = (int)(sizeof(cplx<T>) / sizeof(T));  // map elements per complex
   const int n0 = p0.n();
   const int rows = n0 < 256 ? n0 : 256;  // box height (at most 256)
   cplx<T>* tile = reinterpret_cast<cplx<T>*>(smem_tma);
   cplx<T>* exch = tile + (size_t)DIM * n0 * TB;
-  cplx<T>* tw = exch + (size_t)TB * pitch;
+  cplx<T>* tw = exch + (XS > 0 ? (size_t)0 : (size_t)TB * pitch);
   uint64_t* bar = reinterpret_cast<uint64_t*>(tw + n0);
   const int tb = threadIdx.x % TB, t = threadIdx.x / TB;
   const int64_t b = (int64_t)blockIdx.x * TB + tb;
@@ -742,9 +765,10 @@ __global__ void __launch_bounds__(256)
     if constexpr (PQ) cg_pq_reduce<T>(0.f, 0.0, fp, red);
     return;
   }
-  // The copy destinations must be 128-byte aligned; the launch guarantees
-  // it, and a misplaced window skips the CTA with an error count.
-  if (smem_addr(tile) & 127u) {
+  // The copy destinations must be 128-byte aligned, and in-tile exchanges
+  // need TB = XS; the launch guarantees both, and a misplaced window skips
+  // the CTA with an error count.
+  if ((smem_addr(tile) & 127u) || (XS > 0 && TB != XS)) {
     if (threadIdx.x == 0) {
       atomicAdd(&g_tma_timeouts, 1);
       report_status(fp.status, 1);
@@ -830,6 +854,7 @@ __global__ void __launch_bounds__(256)
     // that pass slower, 80 -> 92 us at 128^3).
     constexpr bool KL = std::is_same<T, float>::value;
     static_assert(!PQ || KL, "p.Kp by Parseval: FP32 only");
+    static_assert(XS == 0 || !KL, "in-tile exchanges: float pairs only");
     float pq = 0.f;  // this thread's modes' Re(conj(p) . K p), PQ only
     cplx<T> v[Eng::E];
 #pragma unroll 1
@@ -837,7 +862,12 @@ __global__ void __launch_bounds__(256)
       cplx<T>* tc = tile + (size_t)c * n0 * TB + tb;
 #pragma unroll
       for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
-      p0.template run<T, false>(v, buf, t, tw, 1);
+      if constexpr (XS > 0) {
+        __syncthreads();
+        p0.template run_strided<T, false, XS>(v, tc, t, tw, 1);
+      } else {
+        p0.template run<T, false>(v, buf, t, tw, 1);
+      }
       if (!KL || c < DIM - 1) {
 #pragma unroll
         for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
@@ -891,7 +921,14 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int q = 0; q < Eng::E; q++) v[q] = tc[(t + p0.T() * q) * TB];
       }
-      p0.template run<T, true>(v, buf, t, tw, 1);
+      if constexpr (XS > 0) {
+        // Also orders every thread's K(k) u(k) writes to this slot before
+        // the first exchange.
+        __syncthreads();
+        p0.template run_strided<T, true, XS>(v, tc, t, tw, 1);
+      } else {
+        p0.template run<T, true>(v, buf, t, tw, 1);
+      }
 #pragma unroll
       for (int q = 0; q < Eng::E; q++) tc[(t + p0.T() * q) * TB] = v[q];
     }
