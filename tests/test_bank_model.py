@@ -130,3 +130,44 @@ def test_pitches_the_design_relies_on():
     assert f(32, 2, 8, False, 8) == base(32) + 2
     # Choices are cached per argument set and stable across calls.
     assert f(128, 8, 8, True, 8) == f(128, 8, 8, True, 8)
+
+
+def _tile_exchange_costs(n, lines, csize, E=8):
+    """Wavefronts of every warp access of the exchanges run inside a staged
+    tile laid out [element][lines] (element p of line b at p * lines + b,
+    no padding), lanes stepping across the lines first -- the float-pair
+    TMA axis-0 pass's in-tile exchanges."""
+    T, radices = _stages(n, E)
+    nthreads = T * lines
+    costs = []
+    for w0 in range(0, nthreads, 32):
+        tids = range(w0, min(w0 + 32, nthreads))
+        Ns = 1
+        for R in radices[:-1]:
+            for m in range(E // R):
+                for r in range(R):
+                    addrs = []
+                    for tid in tids:
+                        line, t = tid % lines, tid // lines
+                        j = t + T * m
+                        jm = j % Ns
+                        addrs.append((((j - jm) * R + jm + r * Ns) * lines + line) * csize)
+                    costs.append(_wavefronts(addrs, csize))
+            for q in range(E):
+                addrs = [((tid // lines + T * q) * lines + tid % lines) * csize for tid in tids]
+                costs.append(_wavefronts(addrs, csize))
+            Ns *= R
+    return costs
+
+
+def test_in_tile_exchanges_take_the_minimum_wavefronts_where_used():
+    """Float pairs (16-byte complex) exchange inside the tile where a tile
+    row is 128 bytes (8 lines, n0 = 64 and 128): every warp access there
+    takes the 4 wavefronts its 512 bytes need.  With 64-byte rows (4 lines,
+    n0 = 256) the first stage's writes fall on half the banks and take 8,
+    which is why that length keeps its exchange buffer."""
+    for n in (64, 128):
+        costs = _tile_exchange_costs(n, 8, 16)
+        assert costs and all(c == 4 for c in costs), (n, sorted(set(costs)))
+    costs = _tile_exchange_costs(256, 4, 16)
+    assert max(costs) == 8 and min(costs) == 4
