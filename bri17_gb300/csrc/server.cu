@@ -542,8 +542,8 @@ int enqueue_residual(Bucket* B, int z, bool x_is_zero) {
     dim3 gm(std::min(red_blocks(B->size), kRedMaxBlocks / 3), 3);
     ks_comp_mean<<<gm, kRedThreads, 0, s>>>(xz, B->size, st, parts);
     ks_sub_mean<<<dim3(g1(B->size), 3), 256, 0, s>>>(xz, B->size, st);
-    // FP64-accurate K x in float pairs where the grid has them (64^3 and
-    // larger power-of-two sides), else on the FP64 pipe.
+    // FP64-accurate K x in float pairs where the grid has them (power-of-two
+    // strided axes 64..512, last axis 128..1024), else on the FP64 pipe.
     int rc = B->op64->residual_df
                  ? apply_accurate_mat_async(B->op64, xz, B->q64 + z * n, B->matdf + 4 * z, s)
                  : apply_stiffness_batched_async(B->op64, 1, xz, B->q64 + z * n,

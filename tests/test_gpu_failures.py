@@ -116,6 +116,40 @@ def test_run_out_wait_fails_the_synchronous_entry_points(zero_wait_limit):
     torch.cuda.synchronize()
 
 
+def test_run_out_wait_in_the_float_pair_pass(zero_wait_limit):
+    """The float-pair TMA axis-0 pass (in-tile exchanges at n0 = 64) reports
+    a wait that ran out as the FP32 pass does: the handle's status is
+    BRI17_ERR_TIMEOUT once, the device count is non-zero, and back at the
+    default limit the float-pair result is within the FP64 bound of the
+    oracle again."""
+    import ctypes
+
+    import torch
+
+    from bri17_gb300 import _lib, set_wait_limit_ns, wait_timeouts
+    shape = (64, 64, 128)
+    h, ho = pair(shape, (1.0, 1.0, 1.0), 1.0, 0.25)
+    h.set_float_pair(True)
+    h.fused_form = "tma"
+    u = np.random.default_rng(5).standard_normal((3,) + shape)
+    u -= u.mean(axis=(1, 2, 3), keepdims=True)
+    ud = to_dev(u)
+    f = torch.empty_like(ud)
+    L = _lib.load()
+    assert h.sync_status() == 0
+    zero_wait_limit()
+    assert L.bri17_apply_stiffness(h.handle, ctypes.c_void_p(ud.data_ptr()),
+                                   ctypes.c_void_p(f.data_ptr()), None) == 0
+    assert h.sync_status() == TIMEOUT
+    assert h.sync_status() == 0  # reported once
+    assert wait_timeouts() > 0
+    set_wait_limit_ns(DEFAULT_LIMIT_NS)
+    wait_timeouts()
+    f = h.apply_stiffness(ud)
+    assert h.sync_status() == 0 and wait_timeouts() == 0
+    assert rel_l2(f.cpu().numpy(), O.apply_stiffness(ho, u)) <= 1e-12
+
+
 _SERVER_CHILD = r"""
 import sys
 import numpy as np

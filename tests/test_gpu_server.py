@@ -193,3 +193,32 @@ def test_copying_submit_with_pageable_buffers():
         assert results[b]["status"] == 0 and results[c]["status"] == 0
         assert np.array_equal(srv.result(b), x)
     srv.close()
+
+
+def test_served_results_at_a_float_pair_side():
+    """Side 128 (the serving benchmark's largest): its bucket computes each
+    slot's FP64 residual in float pairs with that slot's material (the
+    float-pair axis-0 pass with in-tile exchanges), beside a 32^3 bucket
+    on the FP64 pipe.  Each served solution equals its solo mixed solve and
+    the FP64 oracle within the stated tolerance, and its true FP64 residual
+    meets the tolerance."""
+    from bri17_gb300.server import Server
+    rng = np.random.default_rng(29)
+    reqs = _requests(rng, 3, [128, 32, 128])
+    srv = Server(memory_budget_bytes=4 << 30, slots_per_bucket=2)
+    ids = [srv.submit(*r, tol=TOL) for r in reqs]
+    results = {r["id"]: r for r in srv.run_until_idle()}
+    assert sorted(results) == sorted(ids)
+    for rid, (shape, L, mu, nu, tau) in zip(ids, reqs):
+        res = results[rid]
+        assert res["status"] == 0 and res["rel_residual"] <= TOL, res
+        x_srv = srv.result(rid)
+        h, ho = pair(shape, L, mu, nu)
+        b = h.eigenstress_rhs(to_dev(tau))
+        x_solo, info = h.cg_solve(b, tol=TOL, mode="mixed")
+        x_ref = O.eigenstress_solve_half(ho, tau, workers=4)
+        assert rel_l2(x_srv, x_solo.cpu().numpy()) <= SOLUTION_TOL
+        assert rel_l2(x_srv, x_ref) <= SOLUTION_TOL
+        r = b - h.apply_stiffness(to_dev(x_srv))
+        assert float(r.norm() / b.norm()) <= 1.01 * TOL
+    srv.close()
