@@ -485,17 +485,21 @@ static int solve_plain64(bri17_op* op, const double* b, double* x, double tol,
   // which each iteration overwrites anyway) whenever the recursive one has
   // dropped 100x since the last check, and at least every kCheck
   // iterations; the iterate with the smallest true residual is kept.  The
-  // solve succeeds when the true residual meets tol, and stops as
-  // stagnated, returning the kept iterate, when the recursive residual has
-  // met tol but the true one has not, when the true residual has not halved
-  // over kStallChecks checks while the recursive one sits 10x or more below
-  // it (or it has grown past 4x the last halving), over 2 kStallChecks
-  // checks in any case, or when it has grown past 10x its smallest.
+  // solve succeeds when the true residual meets tol.  When the recursive
+  // residual has met tol but the true one has not, the true residual
+  // replaces it and the CG goes on; the solve stops as stagnated, returning
+  // the kept iterate, when that happens again without the true residual
+  // having halved since the replacement, when the true residual has not
+  // halved over kStallChecks checks while the recursive one sits 10x or
+  // more below it (or it has grown past 4x the last halving), over
+  // 2 kStallChecks checks in any case, or when it has grown past 10x its
+  // smallest.
   constexpr int kCheck = 256;
   constexpr int kStallChecks = 4;
   int iters = 0;
   int status = BRI17_ERR_NOT_CONVERGED;
   double best = INFINITY, prog = INFINITY;
+  double replaced = INFINITY;  // squared true residual at the last replacement
   int since_prog = 0;
   bool have_best = false;
   rc = read_state(w);
@@ -535,8 +539,18 @@ static int solve_plain64(bri17_op* op, const double* b, double* x, double tol,
                                      cudaMemcpyDeviceToDevice, s));
     }
     if (rr <= thresh_tol) {  // the recursion met tol, the true residual did not
-      status = BRI17_ERR_STAGNATED;
-      break;
+      if (rt >= 0.25 * replaced) {  // and a replacement did not halve it
+        status = BRI17_ERR_STAGNATED;
+        break;
+      }
+      // Residual replacement (van der Vorst and Ye, 2000): r = b - K x from
+      // the K x just computed, rr = |r|^2, search direction kept; the CG
+      // runs on towards tol from the true residual.
+      replaced = rt;
+      k_residual<<<grid1(n), 256, 0, s>>>(w->r, b, w->q, n);
+      k_reliable_resume<<<1, 1, 0, s>>>(w->st, thresh_tol);
+      w->st_host->rr = rt;
+      continue;
     }
     if (rt < 0.25 * prog) {
       prog = rt;
